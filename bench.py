@@ -1,0 +1,301 @@
+"""Benchmark of the raytracer_3D time-stepping path on GB300.
+
+Workload (N=1): the 32^3 x 32^3 wave field with a mean flow
+U = 0.1 sin(2 pi y/Ly) exp(z/500), log-normal spectrum, CFL 0.4, plain
+binary64 form (1,073,741,824 cells per step).  A step is one forward-Euler
+time step of the whole field (one launch of the fused step kernel).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` = cell-updates/s with the state resident in
+HBM, timed with CUDA events on the library's own stream; `e2e` = the same
+metric through the host-array drop-in call rt_integrate_host (upload,
+step, download each step).  The state (8.6 GB) is far larger than L2, so no
+L2 flush is needed between steps.  N>1 runs N independent replicas, one per
+GPU (the path does not shard), with a barrier and max-over-ranks timing.
+`--impl reference` times the CPU restatement of the reference path on the
+host cores instead (the Fortran reference cannot be built on this machine).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "6D cell-updates/s"
+UNIT = "cell-updates/s"
+B_ALG = {"fp64": 72, "fp32": 36}   # algorithmic bytes per cell-update (E r/w + 6 velocities + 1 rate)
+WORKLOAD = dict(n=(32, 32, 32, 32, 32, 32))
+CPU_SAMPLE_N = (16, 16, 16, 16, 16, 16)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """per-cell DRAM bytes of a kernel from the committed ncu summary"""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(kernel_key)
+    return None if e is None else float(e["bytes_per_cell"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region"""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+def dist_init(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("gloo")
+    return rank, world, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (restatement of the reference path) with OpenMP
+# ---------------------------------------------------------------------------
+def cpu_baseline(steps, warmup=1, n=CPU_SAMPLE_N):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import build_oracle as bo
+    bo.build()
+    from harness import build_oracle
+    from raytracer_3d_gb300 import configs
+    exp = configs.jet_large(n=n)
+    o = build_oracle(exp, threads=True)
+    o.integrate(warmup)
+    t0 = time.perf_counter()
+    o.integrate(steps)
+    dt = time.perf_counter() - t0
+    cells = exp.cells
+    value = cells * steps / dt
+    sample = ("jet_large physics (U=0.1 sin(2 pi y/Ly) exp(z/500), CFL 0.4) on a %s grid, %d steps after %d "
+              "warm-up, padded reference layout, OpenMP over the outer m loop" % ("x".join(map(str, n)), steps, warmup))
+    return {"value": value, "unit": UNIT, "cores": o.threads(), "kind": "port", "sample": sample,
+            "seconds": dt}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def time_steps(model, steps):
+    import torch
+    stream = torch.cuda.ExternalStream(model.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = model.launch_count()
+    e0.record(stream)
+    model.integrate(steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
+
+
+def run_form(precision, n, steps, warmup, dist, e2e_steps):
+    import numpy as np
+    import torch
+    from raytracer_3d_gb300 import configs
+    exp = configs.jet_large(n=n)
+    m = configs.build_model(exp, precision)
+    cells = exp.cells
+    m.integrate(warmup)
+    torch.cuda.synchronize()
+    barrier(dist)
+    with ClockSampler(torch.cuda.current_device()) as cs:
+        secs, launches = time_steps(m, steps)
+    secs = max_over_ranks(dist, secs)
+    out = {"cells": cells, "seconds": secs, "launches": launches, "clocks": cs.summary(), "dt": m.dt}
+    # end to end through the host-array drop-in (rt_integrate_host)
+    if e2e_steps > 0:
+        m.get_state()
+        m.integrate_host()  # warm-up of the host path (pinned staging)
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            m.integrate_host()
+        t1 = time.perf_counter()
+        e2e_secs = max_over_ranks(dist, t1 - t0)
+        out["e2e"] = {"seconds": e2e_secs, "steps": e2e_steps,
+                      "bytes": cells * 8}
+        out["finite"] = bool(np.isfinite(m.E).all())
+    m.close()
+    return out
+
+
+def roofline(precision, cells, seconds_per_launch):
+    peak, src = peaks()
+    achieved = B_ALG[precision] * cells / seconds_per_launch / 1e9
+    tb = profile_traffic("step_%s" % precision)
+    return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src
+            if src == "measured" else "fallback 6.8 TB/s",
+            "traffic": None if tb is None else tb * cells,
+            "alg_bytes_per_cell": B_ALG[precision]}
+
+
+def gpu_arm(args):
+    rank, world, local, dist = dist_init(args.gpus)
+    n = (args.n,) * 6
+    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps)
+    forms = {}
+    if not args.no_fp32:
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0)
+        forms["fp32"] = {"value": f32["cells"] * args.steps * world / f32["seconds"],
+                         "ms_per_step": 1e3 * f32["seconds"] / args.steps,
+                         "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
+                         "clocks": f32["clocks"]}
+    cells = main["cells"]
+    value = cells * args.steps * world / main["seconds"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * main["seconds"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded log-normal spectrum, analytic N(z), U(y,z))",
+        "config": {"workload": "jet_large %d^3x%d^3 plain fp64, CFL 0.4 (dt=%%.6g s)" % (n[0], n[0]) % main["dt"],
+                   "cells": cells, "form": "fp64", "l2": "state 8.6 GB per field >> L2; no flush needed",
+                   "parallelism": "replicas x%d" % world},
+        "roofline": roofline("fp64", cells, main["seconds"] / args.steps),
+        "clocks": main["clocks"],
+        "gpu_launches": main["launches"],
+    }
+    if "e2e" in main:
+        e = main["e2e"]
+        line["e2e"] = {"value": cells * e["steps"] * world / e["seconds"], "unit": UNIT,
+                       "h2d_bytes_per_step": e["bytes"], "d2h_bytes_per_step": e["bytes"],
+                       "api": "rt_integrate_host (padded host array in, stepped array out)"}
+    line["forms"] = forms
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_steps)
+        line["cpu_baseline"].pop("seconds", None)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.steps, warmup=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["seconds"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "jet_large plain fp64 (bounded CPU sample)",
+                                             "sample_grid": "x".join(map(str, CPU_SAMPLE_N))},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        import __graft_entry__ as g
+        g.build()
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

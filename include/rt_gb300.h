@@ -1,0 +1,147 @@
+/*
+ * rt_gb300.h -- C ABI of libraytracer_gb300.so, the GB300 (sm_103a)
+ * implementation of raytracer_3D's time-stepping path.
+ *
+ * The reference path has no plugin or FFI interface: it is a set of
+ * argument-free Fortran subroutines working on module state
+ * (for_src/main_module.f90:41-77).  Each entry point below replaces one of
+ * those subroutines, or the part of one that lies on the path, and is meant
+ * to be bound from Fortran with ISO_C_BINDING (bind(C), c_loc of the full
+ * padded allocatable arrays).
+ *
+ * Conventions
+ *   - Host arrays use the reference layout: Fortran column-major, x fastest,
+ *     every axis padded by onx = 2 ghost cells on both sides
+ *     (main_module.f90:114, :135-223).  A 6D array therefore holds
+ *     (nx+4)(ny+4)(nz+4)(nk+4)(nl+4)(nm+4) doubles, a 3D array
+ *     (nx+4)(ny+4)(nz+4), a 1D grid array n+4.
+ *   - Every function returns 0 (RT_OK) or a negative RT_ERR_* code; the
+ *     message is available from rt_last_error().  The Fortran side calls
+ *     halt_stop (parallel_mpi.f90:223-236) on a nonzero code, the
+ *     reference's convention for fatal errors.
+ *   - The library copies host arrays on set/get and never keeps a host
+ *     pointer.  A handle owns all of its device memory; the model state
+ *     stays on the GPU between calls.
+ *   - One host thread per handle; several handles may coexist.  Each handle
+ *     launches on its own CUDA stream (rt_stream).
+ *   - There is no CPU fallback: without a usable sm_103a GPU rt_create fails.
+ */
+#ifndef RT_GB300_H
+#define RT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RT_OK 0
+#define RT_ERR_ARG (-1)      /* invalid argument or call order          */
+#define RT_ERR_NOMEM (-2)    /* device allocation failed                */
+#define RT_ERR_CUDA (-3)     /* CUDA runtime error                      */
+#define RT_ERR_GRID (-4)     /* grid check failed (calc_grid.f90:260-293) */
+#define RT_ERR_STATE (-5)    /* required earlier call missing           */
+
+#define RT_FP64 0            /* plain binary64 form (reference arithmetic) */
+#define RT_FP32 1            /* binary32 state/fluxes/velocities, binary64
+                                coefficients and budget */
+
+typedef struct rt_handle rt_handle;
+
+/* model sizes, main_module.f90:14-19, :114 */
+typedef struct {
+  int nx, ny, nz, nk, nl, nm; /* interior points; nk, nl, nm even or 1 */
+  int onx;                    /* halo width of the host arrays: must be 2 */
+} rt_dims;
+
+/* model parameters, main_module.f90:20-31 */
+typedef struct {
+  double dt;                  /* time step in s                    */
+  double f0;                  /* Coriolis parameter in 1/s         */
+  double sign_of_omega_i;     /* +1 or -1                          */
+  int enable_upper_reflection;
+  int enable_lower_reflection;
+  int precision;              /* RT_FP64 or RT_FP32                */
+} rt_params;
+
+/* energy budget of diagnose.f90:46-329 (scalars) */
+typedef struct {
+  double eint, mflint, mfl_max;
+  double umax, vmax, wmax, kmax, lmax, mmax;
+  double bfl_xs, bfl_xe, bfl_ys, bfl_ye, bfl_zs, bfl_ze;
+  double bfl_ks, bfl_ke, bfl_ls, bfl_le, bfl_ms, bfl_me;
+  double cfl_x, cfl_y, cfl_z, cfl_k, cfl_l, cfl_m;
+  double residual;
+} rt_budget;
+
+/* identifiers of rt_get_field */
+#define RT_F_XDOT 0
+#define RT_F_YDOT 1
+#define RT_F_ZDOT 2
+#define RT_F_KDOT 3
+#define RT_F_LDOT 4
+#define RT_F_MDOT 5
+#define RT_F_LAMBDA_X 6
+#define RT_F_LAMBDA_Y 7
+#define RT_F_LAMBDA_Z 8
+#define RT_F_LAMBDA 9         /* combined rate used by RT_FP32 */
+
+/* Create a handle: allocate_main_module (main_module.f90:131-238) for the
+ * device side.  Validates sizes as pe_decomposition does
+ * (parallel_mpi.f90:16-25: nk, nl, nm even or one). */
+int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out);
+int rt_destroy(rt_handle* h);
+/* message of the last error on h (or of the last failed rt_create for NULL) */
+const char* rt_last_error(const rt_handle* h);
+
+/* Grid after calc_grid (calc_grid.f90:4-177): padded 1D arrays of the grid
+ * spacings dxt..dmt and wavenumbers kt, lt, mt. */
+int rt_set_grid(rt_handle* h, const double* dxt, const double* dyt, const double* dzt,
+                const double* dkt, const double* dlt, const double* dmt, const double* kt,
+                const double* lt, const double* mt);
+/* Background state of set_initial_conditions: padded 3D Nsqr, U, V. */
+int rt_set_background(rt_handle* h, const double* Nsqr, const double* U, const double* V);
+/* Replaces calc_parameter (calc_parameter.f90:2-264, called at
+ * main.f90:47): dispersion relation, face velocities and growth rates,
+ * computed on the GPU in binary64 and kept there. */
+int rt_calc_parameter(rt_handle* h);
+/* Copy a coefficient field to a padded 6D host array.  Velocities: faces
+ * 0..n of their own axis and the interior of the others; growth rates:
+ * interior.  Other host elements are left untouched. */
+int rt_get_field(rt_handle* h, int which, double* out);
+/* max over interior cells of sum_a max(|v_a(i-1)|,|v_a(i)|)/d_a(i); a
+ * CFL number c gives dt = c / rate */
+int rt_max_rate(rt_handle* h, double* rate);
+/* change dt after creation (e.g. once rt_max_rate is known) */
+int rt_set_dt(rt_handle* h, double dt);
+
+/* Upload / download the wave energy E (padded 6D host array; only the
+ * interior is read or written, ghost cells are refilled every step). */
+int rt_set_state(rt_handle* h, const double* E);
+int rt_get_state(rt_handle* h, double* E);
+
+/* Replaces integrate (integrate.f90:4-271, called at main.f90:70):
+ * nsteps forward-Euler steps on the device-resident state. */
+int rt_integrate(rt_handle* h, int nsteps);
+/* One integrate on a host array, the literal drop-in for the module-state
+ * call: E is uploaded, stepped once and written back (interior). */
+int rt_integrate_host(rt_handle* h, double* E);
+
+/* Budget part of diagnose (diagnose.f90:46-329), for the step taken last.
+ * The 3D outputs are padded host arrays (interior written; NULL skips).
+ * Requires at least one step since rt_set_state. */
+int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int, double* diss_ks,
+                double* diss_ke, double* diss_ls, double* diss_le, double* diss_ms,
+                double* diss_me);
+
+/* cudaStream_t of the handle (as void*), for timing with CUDA events */
+int rt_stream(rt_handle* h, void** stream);
+/* number of kernel launches issued by this handle so far */
+long long rt_launch_count(const rt_handle* h);
+/* bytes of device memory held by the handle */
+long long rt_device_bytes(const rt_handle* h);
+/* library version string */
+const char* rt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

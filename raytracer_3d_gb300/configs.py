@@ -1,0 +1,262 @@
+"""Experiment definitions (the role of for_config/*.f90: set_parameter,
+set_grid, set_initial_conditions) for the workloads this package is measured
+and tested on.
+
+Each experiment is a plain description; `build_model` turns it into a
+`Model` by the reference's setup order (main.f90:36-47).  Inputs are seeded
+and synthetic.  Decisions where the workload text and the reference differ
+are listed in the design doc (open x/y boundaries instead of periodic, symmetric
+m grid, CFL-defined dt).
+"""
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Tuple
+
+import numpy as np
+
+from .grid import ONX
+from .model import Model, zeros_padded
+
+# default-real constants of the reference, widened to binary64
+PI_F = float(np.float32(np.pi))          # main_module.f90:10
+
+
+def f32(x):
+    """A Fortran default-real literal widened to binary64."""
+    return float(np.float32(x))
+
+
+@dataclass
+class Experiment:
+    name: str
+    n: Tuple[int, int, int, int, int, int]
+    d_interior: list
+    f0: float
+    background: Callable            # (model) -> fills model.Nsqr/U/V (padded)
+    initial: Callable               # (model, rng) -> fills model.E
+    steps: int
+    dt: Optional[float] = None
+    cfl: Optional[float] = None
+    sign_of_omega_i: float = 1.0
+    upper: bool = True
+    lower: bool = True
+    fixed: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    seed: int = 1234
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def cells(self):
+        return int(np.prod(self.n))
+
+
+def build_model(exp, precision="fp64"):
+    """set_parameter .. calc_parameter for one experiment; returns a Model
+    with the initial state uploaded and dt fixed (from the CFL number when
+    the experiment gives one)."""
+    m = Model(*exp.n, dt=exp.dt if exp.dt else 1.0, f0=exp.f0, sign_of_omega_i=exp.sign_of_omega_i,
+              enable_upper_reflection=exp.upper, enable_lower_reflection=exp.lower,
+              precision=precision, k_fixed=exp.fixed[0], l_fixed=exp.fixed[1], m_fixed=exp.fixed[2])
+    m.calc_grid(exp.d_interior)
+    exp.background(m)
+    exp.initial(m, np.random.Generator(np.random.PCG64(exp.seed)))
+    m.calc_parameter()
+    if exp.cfl is not None:
+        m.set_dt(exp.cfl / m.max_rate())
+    m.set_state()
+    return m
+
+
+def _mesh3(m):
+    xt, yt, zt = m.grid["x"]["t"], m.grid["y"]["t"], m.grid["z"]["t"]
+    return np.meshgrid(xt, yt, zt, indexing="ij")
+
+
+def _interior(m):
+    return tuple(slice(ONX, ONX + k) for k in m.n)
+
+
+def _packet(m, rng, center, width_cells, amp, noise):
+    """Gaussian packet on the interior (widths in cells of each axis)."""
+    sl = _interior(m)
+    coords = []
+    for a, ax in enumerate(("x", "y", "z", "k", "l", "m")):
+        t = m.grid[ax]["t"][ONX:ONX + m.n[a]]
+        if m.n[a] == 1 or center[a] is None:
+            coords.append(np.zeros(m.n[a]))
+            continue
+        d = m.grid[ax]["dt"][ONX:ONX + m.n[a]]
+        coords.append(((t - center[a]) / (width_cells * d)) ** 2)
+    g = np.zeros(m.n)
+    for a in range(6):
+        shp = [1] * 6
+        shp[a] = m.n[a]
+        g = g + coords[a].reshape(shp)
+    E = amp * np.exp(-0.5 * g)
+    if noise:
+        E = E + rng.uniform(0.0, noise, size=m.n)
+    m.E[sl] = E
+
+
+# ---------------------------------------------------------------------------
+# workload 1: plain FP64 packet, CPU-sized
+# ---------------------------------------------------------------------------
+def packet_small(n=(8, 8, 16, 16, 16, 16), steps=200, seed=1234, Lx=40e3, Ly=40e3, Lz=4000.0,
+                 kmax=2e-3, lmax=2e-3, mmax=5e-2, cfl=0.4):
+    """8x8x16 x 16^3, f=1e-4, N(z)=5e-3 exp(z/1000 m) over 4000 m, no mean
+    flow, Gaussian packet at mid x,y,z and (k0,l0,m0)=(1e-3,0,1e-2), widths
+    2 cells, amplitude 1e-3 plus U(0,1e-8) noise, CFL 0.4."""
+    nx, ny, nz, nk, nl, nm = n
+    d = [np.full(nx, Lx / nx), np.full(ny, Ly / ny), np.full(nz, Lz / nz),
+         np.full(nk, 2 * kmax / nk), np.full(nl, 2 * lmax / nl), np.full(nm, 2 * mmax / nm)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.Nsqr[:] = (5e-3 * np.exp(Z / 1000.0)) ** 2
+        m.U[:] = 0.0
+        m.V[:] = 0.0
+
+    def initial(m, rng):
+        c = (Lx / 2, Ly / 2, -Lz / 2, 1e-3, 0.0, 1e-2)
+        _packet(m, rng, c, 2.0, 1e-3, 1e-8)
+
+    return Experiment("packet_small", tuple(n), d, 1e-4, background, initial, steps, cfl=cfl, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# workloads 2/3: 32^6 with a mean flow
+# ---------------------------------------------------------------------------
+def jet_large(n=(32, 32, 32, 32, 32, 32), steps=100, seed=4321, Lx=160e3, Ly=160e3, Lz=4000.0,
+              kmax=2e-3, lmax=2e-3, mmax=5e-2, cfl=0.4):
+    """32^3 x 32^3, U = 0.1 sin(2 pi y/Ly) exp(z/500) m/s, N and f as the
+    small packet, E = seeded log-normal spectrum in (k,l,m) times a uniform
+    spatial envelope, CFL 0.4."""
+    nx, ny, nz, nk, nl, nm = n
+    d = [np.full(nx, Lx / nx), np.full(ny, Ly / ny), np.full(nz, Lz / nz),
+         np.full(nk, 2 * kmax / nk), np.full(nl, 2 * lmax / nl), np.full(nm, 2 * mmax / nm)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.Nsqr[:] = (5e-3 * np.exp(Z / 1000.0)) ** 2
+        m.U[:] = 0.1 * np.sin(2 * np.pi * Y / Ly) * np.exp(Z / 500.0)
+        m.V[:] = 0.0
+
+    def initial(m, rng):
+        spec = np.exp(0.5 * rng.standard_normal(m.n[3:]))
+        E = 1e-3 * np.broadcast_to(spec[None, None, None], m.n)
+        m.E[_interior(m)] = E
+
+    return Experiment("jet_large", tuple(n), d, 1e-4, background, initial, steps, cfl=cfl, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# small all-axes case with a fully 3D mean flow (exercises every lambda term)
+# ---------------------------------------------------------------------------
+def shear_mini(n=(6, 5, 6, 4, 4, 6), steps=3, seed=7, upper=True, lower=True, cfl=0.4,
+               sign_of_omega_i=1.0):
+    nx, ny, nz, nk, nl, nm = n
+    Lx, Ly, Lz = 30e3, 25e3, 3000.0
+    d = [np.full(nx, Lx / nx), np.full(ny, Ly / ny), np.full(nz, Lz / nz),
+         np.full(nk, 4e-3 / nk), np.full(nl, 4e-3 / nl), np.full(nm, 0.1 / nm)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.Nsqr[:] = (4e-3 * np.exp(Z / 1500.0)) ** 2 * (1 + 0.1 * np.cos(2 * np.pi * X / Lx))
+        m.U[:] = 0.15 * np.sin(2 * np.pi * Y / Ly) * np.exp(Z / 800.0) + 0.02 * np.cos(2 * np.pi * X / Lx)
+        m.V[:] = 0.05 * np.cos(2 * np.pi * X / Lx) * np.exp(Z / 1200.0) + 0.01 * np.sin(2 * np.pi * Y / Ly)
+
+    def initial(m, rng):
+        c = (Lx / 3, Ly / 2, -Lz / 2, 5e-4, -5e-4, 1.5e-2)
+        _packet(m, rng, c, 1.5, 1e-3, 1e-6)
+
+    return Experiment("shear_mini", tuple(n), d, 1.2e-4, background, initial, steps, cfl=cfl, seed=seed,
+                      upper=upper, lower=lower, sign_of_omega_i=sign_of_omega_i)
+
+
+# ---------------------------------------------------------------------------
+# the reference's 1D / 2D test setups (for_config/test1D.f90, test2D.f90):
+# collapsed axes and the analytic-velocity branch
+# ---------------------------------------------------------------------------
+def column_1d(fac=2, steps=3):
+    """test1D: nz=20*fac, nm=60*fac, other axes 1, k_fixed=1e-3 (test1D.f90:3-78)."""
+    nz, nm = int(20 * fac), int(60 * fac)
+    f0 = f32(1e-4)
+    Lx = Ly = Lz = f32(2000.0)
+    n = (1, 1, nz, 1, 1, nm)
+    d = [np.full(1, Lx / 1), np.full(1, Ly / 1), np.full(nz, Lz / nz),
+         np.full(1, PI_F / Lx), np.full(1, PI_F / Ly), np.full(nm, PI_F / Lz / 4.0)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.U[:] = 0.50 * (1 + np.tanh((Z + 750) / 150)) / 2.0
+        m.Nsqr[:] = (30 * f0) ** 2
+        m.V[:] = 0.0
+
+    def initial(m, rng):
+        mt = m.grid["m"]["t"]
+        zt = m.grid["z"]["t"]
+        dmt1 = m.grid["m"]["dt"][ONX]
+        for mm in range(1, nm + 1):
+            if mt[mm + 1] < 0:
+                for kk in range(1, nz + 1):
+                    m.E[ONX, ONX, kk + 1, ONX, ONX, mm + 1] = 1.0 + np.sin(
+                        mt[mm + 1] * 2 * PI_F / (nm * dmt1 / 2 / 6.0)) * np.sin(zt[kk + 1] * 2 * PI_F / (Lz / 6.0))
+
+    return Experiment("column_1d", n, d, f0, background, initial, steps, dt=5.0 / fac,
+                      fixed=(f32(1e-3), 0.0, 0.0))
+
+
+def section_2d(fac=1, steps=3):
+    """test2D: ny=10*fac, nz=20*fac, nl=nm=60*fac, nx=nk=1 (test2D.f90:85-167)."""
+    ny, nz, nl, nm = int(10 * fac), int(20 * fac), int(60 * fac), int(60 * fac)
+    f0 = f32(1e-4)
+    Lz, Ly, Lx = f32(2000.0), f32(20000.0), f32(20000.0)
+    n = (1, ny, nz, 1, nl, nm)
+    d = [np.full(1, Lx / 1), np.full(ny, Ly / ny), np.full(nz, Lz / nz),
+         np.full(1, PI_F / Lx), np.full(nl, 10 * PI_F / Ly), np.full(nm, PI_F / Lz / 4.0)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.U[:] = f32(0.2) * (1 + np.tanh((Z + 750) / 150)) / 2.0 * np.exp(-(Y - Ly / 2.0) ** 2 / 5000 ** 2)
+        m.Nsqr[:] = (30 * f0) ** 2
+        m.V[:] = 0.0
+
+    def initial(m, rng):
+        mt = m.grid["m"]["t"]
+        neg = (mt < 0).astype(np.float64)
+        m.E[:] = neg.reshape((1, 1, 1, 1, 1, -1)) * np.ones(m.E.shape)
+
+    return Experiment("section_2d", n, d, f0, background, initial, steps, dt=40.0 / fac,
+                      fixed=(f32(1e-3), 0.0, 0.0))
+
+
+# ---------------------------------------------------------------------------
+# ensemble member of the batched / served workloads
+# ---------------------------------------------------------------------------
+SPATIAL_DIMS = (8, 16, 24, 32)
+SPECTRAL_DIMS = (8, 12, 16, 24)
+
+
+def ensemble_member(rng, steps=500, spatial=SPATIAL_DIMS, spectral=SPECTRAL_DIMS, cfl=0.4):
+    """One instance: dims per axis drawn from the sets, N0 in [2e-3,1e-2],
+    f in [5e-5,1.4e-4], mean-flow amplitude in [0,0.2] m/s, packet init."""
+    n = tuple(int(rng.choice(spatial)) for _ in range(3)) + tuple(int(rng.choice(spectral)) for _ in range(3))
+    N0 = float(rng.uniform(2e-3, 1e-2))
+    f0 = float(rng.uniform(5e-5, 1.4e-4))
+    amp = float(rng.uniform(0.0, 0.2))
+    seed = int(rng.integers(0, 2 ** 31 - 1))
+    nx, ny, nz, nk, nl, nm = n
+    Lx, Ly, Lz = 5e3 * nx, 5e3 * ny, 4000.0
+    d = [np.full(nx, Lx / nx), np.full(ny, Ly / ny), np.full(nz, Lz / nz),
+         np.full(nk, 4e-3 / nk), np.full(nl, 4e-3 / nl), np.full(nm, 0.1 / nm)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.Nsqr[:] = (N0 * np.exp(Z / 1000.0)) ** 2
+        m.U[:] = amp * np.sin(2 * np.pi * Y / Ly) * np.exp(Z / 500.0)
+        m.V[:] = 0.0
+
+    def initial(m, rng2):
+        c = (Lx / 2, Ly / 2, -Lz / 2, 1e-3, 0.0, 1e-2)
+        _packet(m, rng2, c, 2.0, 1e-3, 1e-8)
+
+    return Experiment("ensemble_member", n, d, f0, background, initial, steps, cfl=cfl, seed=seed,
+                      meta={"N0": N0, "f0": f0, "U_amp": amp})

@@ -1,0 +1,608 @@
+// rt_api.cu -- implementation of the C ABI declared in include/rt_gb300.h.
+//
+// A handle owns, in HBM (unpadded, x fastest):
+//   E[2]        ping-pong state                      T
+//   vel[6]      right-face velocities                T
+//   vlo[6]      face-0 planes                        T
+//   lam[3]      growth rates (FP64: x,y,z; FP32: one combined field)
+//   grid, tab32 padded 1D grids (binary64) and binary32 tables
+//   bg          padded 3D Nsqr, U, V (binary64)
+//   scratch     per-block partial sums of the budget reductions
+// T is double for RT_FP64 and float for RT_FP32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/rt_gb300.h"
+#include "rt_coeff.cuh"
+#include "rt_kernels.h"
+#include "rt_step.cuh"
+
+using namespace rt;
+
+struct rt_handle {
+  Dims d{};
+  rt_params p{};
+  cudaStream_t st = nullptr;
+  int elem = 8;                 // bytes per state/coefficient element
+  double* grid = nullptr;       // 9 padded 1D arrays
+  long long goff[9]{};
+  float* tab32 = nullptr;       // 12 padded 1D arrays
+  long long toff[12]{};
+  double* bg = nullptr;         // 3 padded 3D arrays
+  long long bglen = 0;
+  void* vel[6]{};
+  void* vlo[6]{};
+  void* lam[3]{};
+  void* E[2]{};
+  int cur = 0;
+  double* scratch = nullptr;    // reductions
+  long long scratch_len = 0;
+  double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
+  double* result = nullptr;     // DIAG_RESULT_NV doubles
+  void* pinned = nullptr;       // host staging of one interior field
+  double rate = 0.0;
+  bool have_grid = false, have_bg = false, have_coeff = false, have_state = false;
+  long long steps_since_set = 0;
+  long long launches = 0;
+  long long bytes = 0;
+  std::string err;
+};
+
+static std::string g_create_err;
+
+static int fail(rt_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf; else g_create_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(h, call)                                                              \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(h, RT_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+                  __FILE__, __LINE__);                                                 \
+  } while (0)
+
+static int dev_alloc(rt_handle* h, void** ptr, size_t n) {
+  cudaError_t e = cudaMalloc(ptr, n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(h, RT_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", n, cudaGetErrorString(e));
+  }
+  h->bytes += (long long)n;
+  return RT_OK;
+}
+
+// transient device buffer (not counted in the handle's resident bytes)
+static int tmp_alloc(rt_handle* h, void** ptr, size_t n) {
+  cudaError_t e = cudaMalloc(ptr, n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(h, RT_ERR_NOMEM, "cudaMalloc of %zu bytes (temporary) failed: %s", n,
+                cudaGetErrorString(e));
+  }
+  return RT_OK;
+}
+
+static long long padded_len(const Dims& d, int a) { return d.n[a] + 2 * RT_ONX; }
+
+// ---------------------------------------------------------------------------
+// host gather/scatter between the padded Fortran layout and the compact
+// interior, split over host threads by outer slabs
+// ---------------------------------------------------------------------------
+template <class F>
+static void parallel_slabs(long long nslab, F&& fn) {
+  unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (nslab < 64) nt = 1;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; t++)
+    th.emplace_back([&, t] {
+      for (long long s = t; s < nslab; s += nt) fn(s);
+    });
+  for (auto& x : th) x.join();
+}
+
+template <class T>
+static void gather_interior(const Dims& d, const double* host, T* dst) {
+  long long P[6];
+  for (int a = 0; a < 6; a++) P[a] = padded_len(d, a);
+  const long long nslab = (long long)d.n[2] * d.n[3] * d.n[4] * d.n[5];
+  parallel_slabs(nslab, [&](long long s) {
+    long long r = s;
+    const int k = (int)(r % d.n[2]); r /= d.n[2];
+    const int l = (int)(r % d.n[3]); r /= d.n[3];
+    const int n = (int)(r % d.n[4]);
+    const int m = (int)(r / d.n[4]);
+    for (int j = 0; j < d.n[1]; j++) {
+      const long long src = RT_ONX + P[0] * ((j + RT_ONX) + P[1] * ((k + RT_ONX) + P[2] *
+                            ((l + RT_ONX) + P[3] * ((n + RT_ONX) + P[4] * (long long)(m + RT_ONX)))));
+      const long long dst0 = (long long)d.n[0] * (j + (long long)d.n[1] * s);
+      for (int i = 0; i < d.n[0]; i++) dst[dst0 + i] = (T)host[src + i];
+    }
+  });
+}
+
+template <class T>
+static void scatter_interior(const Dims& d, const T* src, double* host) {
+  long long P[6];
+  for (int a = 0; a < 6; a++) P[a] = padded_len(d, a);
+  const long long nslab = (long long)d.n[2] * d.n[3] * d.n[4] * d.n[5];
+  parallel_slabs(nslab, [&](long long s) {
+    long long r = s;
+    const int k = (int)(r % d.n[2]); r /= d.n[2];
+    const int l = (int)(r % d.n[3]); r /= d.n[3];
+    const int n = (int)(r % d.n[4]);
+    const int m = (int)(r / d.n[4]);
+    for (int j = 0; j < d.n[1]; j++) {
+      const long long dst = RT_ONX + P[0] * ((j + RT_ONX) + P[1] * ((k + RT_ONX) + P[2] *
+                            ((l + RT_ONX) + P[3] * ((n + RT_ONX) + P[4] * (long long)(m + RT_ONX)))));
+      const long long src0 = (long long)d.n[0] * (j + (long long)d.n[1] * s);
+      for (int i = 0; i < d.n[0]; i++) host[dst + i] = (double)src[src0 + i];
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// argument structs for the kernels
+// ---------------------------------------------------------------------------
+static Grid make_grid(const rt_handle* h) {
+  Grid g;
+  for (int a = 0; a < 6; a++) g.d[a] = h->grid + h->goff[a];
+  g.kt = h->grid + h->goff[6];
+  g.lt = h->grid + h->goff[7];
+  g.mt = h->grid + h->goff[8];
+  return g;
+}
+
+template <class T>
+static StepArgs<T> make_step_args(const rt_handle* h, int src) {
+  StepArgs<T> A;
+  A.d = h->d;
+  A.g = make_grid(h);
+  for (int a = 0; a < 6; a++) {
+    A.t32.inv_d[a] = h->tab32 + h->toff[a];
+    A.t32.cfl[a] = h->tab32 + h->toff[6 + a];
+    A.vel[a] = (const T*)h->vel[a];
+    A.vlo[a] = (const T*)h->vlo[a];
+  }
+  for (int c = 0; c < 3; c++) A.lam[c] = (const T*)h->lam[c];
+  A.E = (const T*)h->E[src];
+  A.Enew = (T*)h->E[1 - src];
+  A.dt = h->p.dt;
+  return A;
+}
+
+// binary32 tables 1/d and dt/d on the padded range
+static int upload_tab32(rt_handle* h) {
+  std::vector<double> hg(h->goff[8] + padded_len(h->d, 5));
+  CUDA_TRY(h, cudaMemcpy(hg.data(), h->grid, hg.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<float> t(h->toff[11] + padded_len(h->d, 5));
+  for (int a = 0; a < 6; a++)
+    for (long long i = 0; i < padded_len(h->d, a); i++) {
+      const double dd = hg[h->goff[a] + i];
+      t[h->toff[a] + i] = (float)(1.0 / dd);
+      t[h->toff[6 + a] + i] = (float)(h->p.dt / dd);
+    }
+  CUDA_TRY(h, cudaMemcpy(h->tab32, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* rt_version(void) { return "raytracer_gb300 0.1 (sm_103a)"; }
+
+const char* rt_last_error(const rt_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
+  if (!dims || !params || !out) return fail(nullptr, RT_ERR_ARG, "rt_create: NULL argument");
+  *out = nullptr;
+  const int nn[6] = {dims->nx, dims->ny, dims->nz, dims->nk, dims->nl, dims->nm};
+  for (int a = 0; a < 6; a++)
+    if (nn[a] < 1) return fail(nullptr, RT_ERR_ARG, "rt_create: axis %d has %d points", a, nn[a]);
+  if (dims->onx != RT_ONX)
+    return fail(nullptr, RT_ERR_ARG, "rt_create: onx must be %d (main_module.f90:114), got %d",
+                RT_ONX, dims->onx);
+  // parallel_mpi.f90:16-25
+  if (dims->nk > 1 && dims->nk % 2) return fail(nullptr, RT_ERR_ARG, " nk must be even or one ");
+  if (dims->nl > 1 && dims->nl % 2) return fail(nullptr, RT_ERR_ARG, " nl must be even or one ");
+  if (dims->nm > 1 && dims->nm % 2) return fail(nullptr, RT_ERR_ARG, " nm must be even or one");
+  if (params->precision != RT_FP64 && params->precision != RT_FP32)
+    return fail(nullptr, RT_ERR_ARG, "rt_create: unknown precision %d", params->precision);
+  if (!(params->dt > 0.0)) return fail(nullptr, RT_ERR_ARG, "rt_create: dt must be > 0");
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, RT_ERR_CUDA, "rt_create: no CUDA device: %s", cudaGetErrorString(ce));
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.major * 10 + prop.minor < 100) {
+    cudaGetLastError();
+    return fail(nullptr, RT_ERR_CUDA, "rt_create: device %d is not a Blackwell GPU", dev);
+  }
+
+  rt_handle* h = new rt_handle();
+  h->p = *params;
+  Dims& d = h->d;
+  long long st = 1;
+  for (int a = 0; a < 6; a++) {
+    d.n[a] = nn[a];
+    d.s[a] = st;
+    st *= nn[a];
+  }
+  d.ncell = st;
+  d.nvol3 = (long long)nn[0] * nn[1] * nn[2];
+  d.nspec = (long long)nn[3] * nn[4] * nn[5];
+  d.upper_refl = params->enable_upper_reflection ? 1 : 0;
+  d.lower_refl = params->enable_lower_reflection ? 1 : 0;
+  h->elem = params->precision == RT_FP64 ? 8 : 4;
+
+  auto bail = [&](int code) {
+    g_create_err = h->err;
+    rt_destroy(h);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(h, RT_ERR_CUDA, "rt_create: stream creation failed"));
+
+  long long gl = 0;
+  for (int a = 0; a < 6; a++) { h->goff[a] = gl; gl += padded_len(d, a); }
+  for (int c = 0; c < 3; c++) { h->goff[6 + c] = gl; gl += padded_len(d, 3 + c); }
+  long long tl = 0;
+  for (int k = 0; k < 12; k++) { h->toff[k] = tl; tl += padded_len(d, k % 6); }
+  h->bglen = padded_len(d, 0) * padded_len(d, 1) * padded_len(d, 2);
+  int rc;
+  if ((rc = dev_alloc(h, (void**)&h->grid, gl * sizeof(double)))) return bail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->tab32, tl * sizeof(float)))) return bail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->bg, 3 * h->bglen * sizeof(double)))) return bail(rc);
+  const size_t fb = (size_t)d.ncell * h->elem;
+  for (int k = 0; k < 2; k++)
+    if ((rc = dev_alloc(h, &h->E[k], fb))) return bail(rc);
+  for (int a = 0; a < 6; a++) {
+    if ((rc = dev_alloc(h, &h->vel[a], fb))) return bail(rc);
+    if ((rc = dev_alloc(h, &h->vlo[a], (size_t)(d.ncell / d.n[a]) * h->elem))) return bail(rc);
+  }
+  const int nlam = params->precision == RT_FP64 ? 3 : 1;
+  for (int c = 0; c < nlam; c++)
+    if ((rc = dev_alloc(h, &h->lam[c], fb))) return bail(rc);
+  const DiagSizes ds = diag_sizes(d);
+  h->scratch_len = std::max(ds.scratch_doubles(), max_rate_partials(d)) + 8;
+  if ((rc = dev_alloc(h, (void**)&h->scratch, h->scratch_len * sizeof(double)))) return bail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->vol3, 8 * d.nvol3 * sizeof(double)))) return bail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->result, 32 * sizeof(double)))) return bail(rc);
+  *out = h;
+  return RT_OK;
+}
+
+int rt_destroy(rt_handle* h) {
+  if (!h) return RT_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  cudaFree(h->grid);
+  cudaFree(h->tab32);
+  cudaFree(h->bg);
+  for (int k = 0; k < 2; k++) cudaFree(h->E[k]);
+  for (int a = 0; a < 6; a++) { cudaFree(h->vel[a]); cudaFree(h->vlo[a]); }
+  for (int c = 0; c < 3; c++) cudaFree(h->lam[c]);
+  cudaFree(h->scratch);
+  cudaFree(h->vol3);
+  cudaFree(h->result);
+  if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return RT_OK;
+}
+
+int rt_set_grid(rt_handle* h, const double* dxt, const double* dyt, const double* dzt,
+                const double* dkt, const double* dlt, const double* dmt, const double* kt,
+                const double* lt, const double* mt) {
+  if (!h) return RT_ERR_ARG;
+  const double* src[9] = {dxt, dyt, dzt, dkt, dlt, dmt, kt, lt, mt};
+  for (int k = 0; k < 9; k++) {
+    if (!src[k]) return fail(h, RT_ERR_ARG, "rt_set_grid: array %d is NULL", k);
+    const int a = k < 6 ? k : k - 3;
+    const long long n = padded_len(h->d, a);
+    if (k < 6)
+      for (long long i = 0; i < n; i++)
+        if (!(src[k][i] > 0.0))
+          return fail(h, RT_ERR_GRID, "rt_set_grid: spacing %d at padded index %lld is not > 0", k, i);
+    CUDA_TRY(h, cudaMemcpy(h->grid + h->goff[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  int rc = upload_tab32(h);
+  if (rc) return rc;
+  h->have_grid = true;
+  h->have_coeff = false;
+  return RT_OK;
+}
+
+int rt_set_background(rt_handle* h, const double* Nsqr, const double* U, const double* V) {
+  if (!h) return RT_ERR_ARG;
+  if (!Nsqr || !U || !V) return fail(h, RT_ERR_ARG, "rt_set_background: NULL array");
+  const double* src[3] = {Nsqr, U, V};
+  for (int k = 0; k < 3; k++)
+    CUDA_TRY(h, cudaMemcpy(h->bg + k * h->bglen, src[k], h->bglen * sizeof(double),
+                           cudaMemcpyHostToDevice));
+  h->have_bg = true;
+  h->have_coeff = false;
+  return RT_OK;
+}
+
+int rt_set_dt(rt_handle* h, double dt) {
+  if (!h) return RT_ERR_ARG;
+  if (!(dt > 0.0)) return fail(h, RT_ERR_ARG, "rt_set_dt: dt must be > 0");
+  h->p.dt = dt;
+  if (h->have_grid) return upload_tab32(h);
+  return RT_OK;
+}
+
+int rt_calc_parameter(rt_handle* h) {
+  if (!h) return RT_ERR_ARG;
+  if (!h->have_grid || !h->have_bg)
+    return fail(h, RT_ERR_STATE, "rt_calc_parameter: rt_set_grid and rt_set_background first");
+  const Dims& d = h->d;
+  Background bg;
+  bg.Nsqr = h->bg;
+  bg.U = h->bg + h->bglen;
+  bg.V = h->bg + 2 * h->bglen;
+  bg.px = (int)padded_len(d, 0);
+  bg.py = (int)padded_len(d, 1);
+  Phys ph{h->p.f0, h->p.sign_of_omega_i, h->p.dt};
+  const Grid g = make_grid(h);
+
+  CoeffOut64 o64{};
+  std::vector<void*> tmp;
+  const bool fp64 = h->p.precision == RT_FP64;
+  int rc;
+  // binary64 destinations: the handle's own fields (FP64) or temporaries
+  for (int a = 0; a < 6; a++) {
+    if (fp64) {
+      o64.vel[a] = (double*)h->vel[a];
+      o64.vlo[a] = (double*)h->vlo[a];
+    } else {
+      void* p1 = nullptr; void* p2 = nullptr;
+      if ((rc = tmp_alloc(h, &p1, d.ncell * sizeof(double)))) goto cleanup;
+      tmp.push_back(p1);
+      if ((rc = tmp_alloc(h, &p2, (d.ncell / d.n[a]) * sizeof(double)))) goto cleanup;
+      tmp.push_back(p2);
+      o64.vel[a] = (double*)p1;
+      o64.vlo[a] = (double*)p2;
+    }
+  }
+  for (int c = 0; c < 3; c++) {
+    if (fp64) {
+      o64.lam[c] = (double*)h->lam[c];
+    } else {
+      void* p1 = nullptr;
+      if ((rc = tmp_alloc(h, &p1, d.ncell * sizeof(double)))) goto cleanup;
+      tmp.push_back(p1);
+      o64.lam[c] = (double*)p1;
+    }
+  }
+  {
+    cudaError_t e = launch_coeff(d, bg, g, ph, o64, h->st);
+    h->launches += 7;
+    if (e != cudaSuccess) { rc = fail(h, RT_ERR_CUDA, "coefficients: %s", cudaGetErrorString(e)); goto cleanup; }
+    ConstCoeff64 cf;
+    for (int a = 0; a < 6; a++) { cf.vel[a] = o64.vel[a]; cf.vlo[a] = o64.vlo[a]; }
+    e = launch_max_rate(d, g, cf, h->scratch, h->result, h->st);
+    h->launches += 2;
+    if (e != cudaSuccess) { rc = fail(h, RT_ERR_CUDA, "max rate: %s", cudaGetErrorString(e)); goto cleanup; }
+    if (!fp64) {
+      for (int a = 0; a < 6; a++) {
+        if ((e = launch_to_fp32(o64.vel[a], (float*)h->vel[a], d.ncell, h->st)) != cudaSuccess) break;
+        if ((e = launch_to_fp32(o64.vlo[a], (float*)h->vlo[a], d.ncell / d.n[a], h->st)) != cudaSuccess) break;
+        h->launches += 2;
+      }
+      if (e == cudaSuccess)
+        e = launch_lam_combine(o64.lam[0], o64.lam[1], o64.lam[2], d.n[0] > 1, d.n[1] > 1,
+                               d.n[2] > 1, (float*)h->lam[0], d.ncell, h->st);
+      h->launches += 1;
+      if (e != cudaSuccess) { rc = fail(h, RT_ERR_CUDA, "fp32 conversion: %s", cudaGetErrorString(e)); goto cleanup; }
+    }
+    e = cudaMemcpyAsync(&h->rate, h->result, sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) { rc = fail(h, RT_ERR_CUDA, "calc_parameter: %s", cudaGetErrorString(e)); goto cleanup; }
+  }
+  rc = RT_OK;
+  h->have_coeff = true;
+cleanup:
+  cudaStreamSynchronize(h->st);  // no kernel may still read a temporary
+  for (void* p : tmp) { cudaFree(p); }
+  return rc;
+}
+
+int rt_max_rate(rt_handle* h, double* rate) {
+  if (!h || !rate) return RT_ERR_ARG;
+  if (!h->have_coeff) return fail(h, RT_ERR_STATE, "rt_max_rate: rt_calc_parameter first");
+  *rate = h->rate;
+  return RT_OK;
+}
+
+static int ensure_pinned(rt_handle* h) {
+  if (h->pinned) return RT_OK;
+  cudaError_t e = cudaHostAlloc(&h->pinned, (size_t)h->d.ncell * 8, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->pinned = nullptr;
+    return fail(h, RT_ERR_NOMEM, "pinned staging allocation failed: %s", cudaGetErrorString(e));
+  }
+  return RT_OK;
+}
+
+int rt_get_field(rt_handle* h, int which, double* out) {
+  if (!h || !out) return RT_ERR_ARG;
+  if (!h->have_coeff) return fail(h, RT_ERR_STATE, "rt_get_field: rt_calc_parameter first");
+  const Dims& d = h->d;
+  const bool fp64 = h->p.precision == RT_FP64;
+  const void* src = nullptr;
+  if (which >= RT_F_XDOT && which <= RT_F_MDOT) src = h->vel[which];
+  else if (which >= RT_F_LAMBDA_X && which <= RT_F_LAMBDA_Z && fp64) src = h->lam[which - RT_F_LAMBDA_X];
+  else if (which == RT_F_LAMBDA && !fp64) src = h->lam[0];
+  else return fail(h, RT_ERR_ARG, "rt_get_field: field %d not available in this precision", which);
+  int rc = ensure_pinned(h);
+  if (rc) return rc;
+  CUDA_TRY(h, cudaMemcpyAsync(h->pinned, src, (size_t)d.ncell * h->elem, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  if (fp64) scatter_interior<double>(d, (const double*)h->pinned, out);
+  else scatter_interior<float>(d, (const float*)h->pinned, out);
+  if (which <= RT_F_MDOT) {
+    // face 0 of the velocity's own axis lives in the plane vlo[a]
+    const int a = which;
+    const long long np = d.ncell / d.n[a];
+    std::vector<double> pl(np);
+    if (fp64) {
+      CUDA_TRY(h, cudaMemcpy(pl.data(), h->vlo[a], np * 8, cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<float> pf(np);
+      CUDA_TRY(h, cudaMemcpy(pf.data(), h->vlo[a], np * 4, cudaMemcpyDeviceToHost));
+      for (long long q = 0; q < np; q++) pl[q] = pf[q];
+    }
+    long long P[6];
+    for (int b = 0; b < 6; b++) P[b] = padded_len(d, b);
+    for (long long q = 0; q < np; q++) {
+      long long r = q, idx = 0, stp = 1;
+      for (int b = 0; b < 6; b++) {
+        int f;  // Fortran index
+        if (b == a) f = 0;
+        else { f = (int)(r % d.n[b]) + 1; r /= d.n[b]; }
+        idx += (long long)(f + RT_ONX - 1) * stp;
+        stp *= P[b];
+      }
+      out[idx] = pl[q];
+    }
+  }
+  return RT_OK;
+}
+
+int rt_set_state(rt_handle* h, const double* E) {
+  if (!h || !E) return RT_ERR_ARG;
+  int rc = ensure_pinned(h);
+  if (rc) return rc;
+  const Dims& d = h->d;
+  if (h->p.precision == RT_FP64) gather_interior<double>(d, E, (double*)h->pinned);
+  else gather_interior<float>(d, E, (float*)h->pinned);
+  h->cur = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(h->E[0], h->pinned, (size_t)d.ncell * h->elem, cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  h->have_state = true;
+  h->steps_since_set = 0;
+  return RT_OK;
+}
+
+int rt_get_state(rt_handle* h, double* E) {
+  if (!h || !E) return RT_ERR_ARG;
+  if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_get_state: no state (rt_set_state first)");
+  int rc = ensure_pinned(h);
+  if (rc) return rc;
+  const Dims& d = h->d;
+  CUDA_TRY(h, cudaMemcpyAsync(h->pinned, h->E[h->cur], (size_t)d.ncell * h->elem, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  if (h->p.precision == RT_FP64) scatter_interior<double>(d, (const double*)h->pinned, E);
+  else scatter_interior<float>(d, (const float*)h->pinned, E);
+  return RT_OK;
+}
+
+int rt_integrate(rt_handle* h, int nsteps) {
+  if (!h) return RT_ERR_ARG;
+  if (nsteps < 0) return fail(h, RT_ERR_ARG, "rt_integrate: nsteps < 0");
+  if (!h->have_coeff) return fail(h, RT_ERR_STATE, "rt_integrate: rt_calc_parameter first");
+  if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_integrate: rt_set_state first");
+  for (int t = 0; t < nsteps; t++) {
+    cudaError_t e;
+    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->st);
+    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->st);
+    h->launches += 1;
+    if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    h->cur = 1 - h->cur;
+    h->steps_since_set += 1;
+  }
+  return RT_OK;
+}
+
+int rt_integrate_host(rt_handle* h, double* E) {
+  int rc = rt_set_state(h, E);
+  if (rc) return rc;
+  if ((rc = rt_integrate(h, 1))) return rc;
+  return rt_get_state(h, E);
+}
+
+int rt_diagnose(rt_handle* h, rt_budget* o, double* E_int, double* meanfl_int, double* diss_ks,
+                double* diss_ke, double* diss_ls, double* diss_le, double* diss_ms,
+                double* diss_me) {
+  if (!h || !o) return RT_ERR_ARG;
+  if (!h->have_state || h->steps_since_set < 1)
+    return fail(h, RT_ERR_STATE, "rt_diagnose: needs a step since rt_set_state (diagnose follows integrate, main.f90:70-74)");
+  const Dims& d = h->d;
+  const int prev = 1 - h->cur;  // state before the last step
+  cudaError_t e;
+  if (h->p.precision == RT_FP64)
+    e = launch_diag<double>(make_step_args<double>(h, prev), (const double*)h->E[h->cur], h->scratch,
+                            h->vol3, h->result, h->st);
+  else
+    e = launch_diag<float>(make_step_args<float>(h, prev), (const float*)h->E[h->cur], h->scratch,
+                           h->vol3, h->result, h->st);
+  h->launches += 4;
+  if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "diagnose launch: %s", cudaGetErrorString(e));
+  double r[DIAG_RESULT_NV];
+  CUDA_TRY(h, cudaMemcpyAsync(r, h->result, sizeof(r), cudaMemcpyDeviceToHost, h->st));
+  std::vector<double> v3((size_t)8 * d.nvol3);
+  CUDA_TRY(h, cudaMemcpyAsync(v3.data(), h->vol3, v3.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  o->eint = r[0]; o->mflint = r[1]; o->mfl_max = r[2];
+  o->umax = r[3]; o->vmax = r[4]; o->wmax = r[5]; o->kmax = r[6]; o->lmax = r[7]; o->mmax = r[8];
+  double* b = &o->bfl_xs;
+  for (int k = 0; k < 12; k++) b[k] = r[DIAG_CELL_NV + k];
+  // CFL, diagnose.f90:295-313
+  const double vmx[6] = {o->umax, o->vmax, o->wmax, o->kmax, o->lmax, o->mmax};
+  double* cfl = &o->cfl_x;
+  std::vector<double> hg(h->goff[8] + padded_len(d, 5));
+  CUDA_TRY(h, cudaMemcpy(hg.data(), h->grid, hg.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int a = 0; a < 6; a++) {
+    double c = 0;
+    for (int i = 1; i <= d.n[a]; i++) {
+      const double x = vmx[a] * h->p.dt / hg[h->goff[a] + i + RT_ONX - 1];
+      c = c > x ? c : x;
+    }
+    cfl[a] = c;
+  }
+  // diagnose.f90:327-328
+  o->residual = o->eint + o->mflint + o->bfl_xe + o->bfl_ye + o->bfl_ze + o->bfl_ke + o->bfl_le +
+                o->bfl_me - o->bfl_xs - o->bfl_ys - o->bfl_zs - o->bfl_ks - o->bfl_ls - o->bfl_ms;
+  double* outs[8] = {E_int, meanfl_int, diss_ks, diss_ke, diss_ls, diss_le, diss_ms, diss_me};
+  const long long P0 = padded_len(d, 0), P1 = padded_len(d, 1);
+  for (int f = 0; f < 8; f++) {
+    if (!outs[f]) continue;
+    for (long long q = 0; q < d.nvol3; q++) {
+      const int i = (int)(q % d.n[0]), j = (int)((q / d.n[0]) % d.n[1]), k = (int)(q / ((long long)d.n[0] * d.n[1]));
+      outs[f][(i + RT_ONX) + P0 * ((j + RT_ONX) + P1 * (long long)(k + RT_ONX))] = v3[(size_t)f * d.nvol3 + q];
+    }
+  }
+  return RT_OK;
+}
+
+int rt_stream(rt_handle* h, void** stream) {
+  if (!h || !stream) return RT_ERR_ARG;
+  *stream = (void*)h->st;
+  return RT_OK;
+}
+
+long long rt_launch_count(const rt_handle* h) { return h ? h->launches : 0; }
+long long rt_device_bytes(const rt_handle* h) { return h ? h->bytes : 0; }
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// rt_kernels.h -- host-visible launchers of the sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rt_common.cuh"
+
+namespace rt {
+
+struct Phys;
+template <class T> struct StepArgs;
+
+// binary32 literal 1e-12 of diagnose.f90:56, widened to binary64
+#define RT_LIT_1EM12 9.9999999600419720e-13
+
+// number of per-block values of the cell reduction: eint, mflint, mfl_max,
+// umax, vmax, wmax, kmax, lmax, mmax
+#define DIAG_CELL_NV 9
+// result vector of launch_diag: DIAG_CELL_NV cell values, then
+// bfl_xs, bfl_xe, bfl_ys, bfl_ye, ..., bfl_ms, bfl_me
+#define DIAG_RESULT_NV (DIAG_CELL_NV + 12)
+
+struct CoeffOut64 {
+  double* vel[6];
+  double* vlo[6];
+  double* lam[3];
+};
+
+struct ConstCoeff64 {
+  const double* vel[6];
+  const double* vlo[6];
+};
+
+struct DiagSizes {
+  long long cell_blocks;
+  long long plane_blocks;
+  long long scratch_doubles() const { return cell_blocks * DIAG_CELL_NV + 6 * plane_blocks * 2; }
+};
+
+// grid spacing of 0-based cell c along axis a
+__host__ __device__ __forceinline__ double g_d(const Grid& g, int a, int c) { return g.d[a][pidx(c + 1)]; }
+
+cudaError_t launch_coeff(const Dims& d, const Background& bg, const Grid& g, const Phys& ph,
+                         const CoeffOut64& out, cudaStream_t st);
+long long max_rate_partials(const Dims& d);
+cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf, double* partial,
+                            double* out, cudaStream_t st);
+cudaError_t launch_to_fp32(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_lam_combine(const double* lx, const double* ly, const double* lz, int ux, int uy,
+                               int uz, float* dst, long long n, cudaStream_t st);
+template <class T>
+cudaError_t launch_step(const StepArgs<T>& A, cudaStream_t st);
+DiagSizes diag_sizes(const Dims& d);
+template <class T>
+cudaError_t launch_diag(const StepArgs<T>& A, const T* Ecur, double* scratch, double* vol3,
+                        double* result, cudaStream_t st);
+
+}  // namespace rt

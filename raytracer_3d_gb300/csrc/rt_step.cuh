@@ -1,0 +1,154 @@
+// rt_step.cuh -- the fused time step: superbee face fluxes
+// (superbee_fluxes.f90:4-174), flux divergence (integrate.f90:105-200),
+// mean-flow term (:202-252) and forward-Euler update (:255-268) in one
+// sweep over E.  Fluxes, dE and meanfl are never stored.
+#pragma once
+#include "rt_common.cuh"
+
+namespace rt {
+
+// binary32 literal 1.E20 of superbee_fluxes.f90:26, widened to binary64
+#define RT_LIT_1E20 1.0000000200408773e20
+
+// ---- plain binary64 form: the reference's arithmetic, bit for bit -------
+// Face flux at face f of one axis from E(f-1), E(f), E(f+1), E(f+2),
+// superbee_fluxes.f90:19-30.
+__device__ __forceinline__ double flux_fp64(double v, double dgrid, double dt, double Ea, double Eb,
+                                            double Ec, double Ed) {
+  const double uCFL = fabs(ddiv(dmul(v, dt), dgrid));
+  const double Rjp = dsub(Ed, Ec);
+  const double Rj = dsub(Ec, Eb);
+  const double Rjm = dsub(Eb, Ea);
+  const double up = v > 0 ? Rjm : Rjp;
+  double Cr = (Rj != 0.0) ? ddiv(up, Rj) : dmul(up, RT_LIT_1E20);
+  Cr = fmax2(0.0, fmax2(fmin2(1.0, dmul(2.0, Cr)), fmin2(2.0, Cr)));  // Limiter, :10
+  const double adv = dmul(dmul(v, dadd(Ec, Eb)), 0.5);
+  const double dif = dmul(dmul(dmul(fabs(v), dadd(dsub(1.0, Cr), dmul(uCFL, Cr))), Rj), 0.5);
+  return dsub(adv, dif);
+}
+
+// ---- binary32 precision form -------------------------------------------
+// Same flux with the limiter written without a division: for Rj != 0,
+// phi(r)*Rj with r = up/Rj equals s*max(0, min(|Rj|, 2t), min(2|Rj|, t)),
+// s = sign(Rj), t = s*up; for Rj == 0 the diffusive term vanishes exactly
+// as in the reference (it is multiplied by Rj).  cfl = dt/d(f).
+__device__ __forceinline__ float flux_fp32(float v, float cfl, float Ea, float Eb, float Ec, float Ed) {
+  const float Rjp = Ed - Ec;
+  const float Rj = Ec - Eb;
+  const float Rjm = Eb - Ea;
+  const float up = v > 0.f ? Rjm : Rjp;
+  const float a = fabsf(Rj);
+  const float t = Rj >= 0.f ? up : -up;
+  const float ph = fmaxf(0.f, fmaxf(fminf(a, 2.f * t), fminf(2.f * a, t)));
+  const float psi = Rj >= 0.f ? ph : -ph;
+  const float av = fabsf(v);
+  const float uCFL = av * cfl;
+  const float dif = av * (Rj - (1.f - uCFL) * psi);
+  return 0.5f * (v * (Ec + Eb) - dif);
+}
+
+// Per-axis small tables of the binary32 form: 1/d(f) and dt/d(f) on the
+// padded index range (Fortran index f at position f+1).
+struct Tab32 {
+  const float* inv_d[6];
+  const float* cfl[6];
+};
+
+template <class T>
+struct StepArgs {
+  Dims d;
+  Grid g;
+  Tab32 t32;
+  const T* E;          // state at the start of the step
+  T* Enew;             // state after the step (ping-pong)
+  const T* vel[6];     // right-face velocities
+  const T* vlo[6];     // face-0 planes
+  const T* lam[3];     // fp64: lambda_x/y/z; fp32: lam[0] = combined rate
+  double dt;
+};
+
+// Read E at cell p displaced by off along axis a from coordinate c,
+// applying the ghost-cell map (returns the mapped linear index).
+__device__ __forceinline__ long long nb_index(const Dims& d, long long p, int a, int c, int off,
+                                              int cm) {
+  int flip = 0;
+  const int c2 = map_coord(d, a, c + off, flip);
+  long long q = p + (long long)(c2 - c) * d.s[a];
+  if (flip) q += (long long)((d.n[5] - 1 - cm) - cm) * d.s[5];
+  return q;
+}
+
+// Per-cell tendency (everything but the update), shared by the step and the
+// budget kernels so that both see bit-identical dE and meanfl.
+template <class T>
+struct CellTerms {
+  T dE;        // -(flux divergence), before the mean-flow term
+  T meanfl;
+};
+
+__device__ __forceinline__ long long plane_index(const Dims& d, int a, const int c[6]) {
+  long long q = 0;
+#pragma unroll
+  for (int b = 0; b < 6; b++) q += (long long)c[b] * plane_stride(d, a, b);
+  return q;
+}
+
+template <class T>
+__device__ __forceinline__ CellTerms<T> cell_terms(const StepArgs<T>& A, long long p, const int c[6],
+                                                   T e0);
+
+template <>
+__device__ __forceinline__ CellTerms<double> cell_terms<double>(const StepArgs<double>& A,
+                                                                long long p, const int c[6],
+                                                                double e0) {
+  const Dims& d = A.d;
+  double dE = 0.;
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    if (d.n[a] <= 1) continue;
+    const int ca = c[a];
+    const double Em2 = A.E[nb_index(d, p, a, ca, -2, c[5])];
+    const double Em1 = A.E[nb_index(d, p, a, ca, -1, c[5])];
+    const double Ep1 = A.E[nb_index(d, p, a, ca, +1, c[5])];
+    const double Ep2 = A.E[nb_index(d, p, a, ca, +2, c[5])];
+    const int F = ca + 1;  // Fortran index of the cell = its right face
+    const double vr = A.vel[a][p];
+    const double vl = ca > 0 ? A.vel[a][p - d.s[a]] : A.vlo[a][plane_index(d, a, c)];
+    const double dr = A.g.d[a][pidx(F)];
+    const double dl = A.g.d[a][pidx(F - 1)];
+    const double fr = flux_fp64(vr, dr, A.dt, Em1, e0, Ep1, Ep2);
+    const double fl = flux_fp64(vl, dl, A.dt, Em2, Em1, e0, Ep1);
+    dE = dsub(dE, ddiv(dsub(fr, fl), dr));
+  }
+  double mf = 0.;
+  if (d.n[0] > 1) mf = dadd(mf, dmul(e0, A.lam[0][p]));
+  if (d.n[1] > 1) mf = dadd(mf, dmul(e0, A.lam[1][p]));
+  if (d.n[2] > 1) mf = dadd(mf, dmul(e0, A.lam[2][p]));
+  return {dE, mf};
+}
+
+template <>
+__device__ __forceinline__ CellTerms<float> cell_terms<float>(const StepArgs<float>& A, long long p,
+                                                              const int c[6], float e0) {
+  const Dims& d = A.d;
+  float dE = 0.f;
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    if (d.n[a] <= 1) continue;
+    const int ca = c[a];
+    const float Em2 = A.E[nb_index(d, p, a, ca, -2, c[5])];
+    const float Em1 = A.E[nb_index(d, p, a, ca, -1, c[5])];
+    const float Ep1 = A.E[nb_index(d, p, a, ca, +1, c[5])];
+    const float Ep2 = A.E[nb_index(d, p, a, ca, +2, c[5])];
+    const int F = ca + 1;
+    const float vr = A.vel[a][p];
+    const float vl = ca > 0 ? A.vel[a][p - d.s[a]] : A.vlo[a][plane_index(d, a, c)];
+    const float fr = flux_fp32(vr, A.t32.cfl[a][pidx(F)], Em1, e0, Ep1, Ep2);
+    const float fl = flux_fp32(vl, A.t32.cfl[a][pidx(F - 1)], Em2, Em1, e0, Ep1);
+    dE -= (fr - fl) * A.t32.inv_d[a][pidx(F)];
+  }
+  const float mf = e0 * A.lam[0][p];
+  return {dE, mf};
+}
+
+}  // namespace rt

@@ -1,0 +1,178 @@
+"""Host-side mirror of the reference driver's module-state interface.
+
+The reference keeps its model in module variables (for_src/main_module.f90:
+41-77) and steps it with argument-free subroutines called from the main
+loop (for_src/main.f90:36-79):
+
+    set_parameter; allocate_main_module; set_grid; calc_grid;
+    set_initial_conditions; calc_parameter
+    do: set_forcing; integrate; diagnose (every snapint/dt steps)
+
+`Model` holds the same host arrays (padded, Fortran order) and exposes the
+same steps, with calc_parameter / integrate / the diagnose budget executed
+by libraytracer_gb300.so on the GPU.  Host arrays are numpy float64 in
+Fortran order so that a 6D array indexes as E[i, j, k, l, n, m] with Fortran
+index f at position f + 1.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .grid import AXES, ONX, calc_grid
+
+PRECISIONS = {"fp64": _lib.RT_FP64, "fp32": _lib.RT_FP32}
+
+
+def padded_shape(n):
+    return tuple(int(x) + 2 * ONX for x in n)
+
+
+def zeros_padded(n):
+    return np.zeros(padded_shape(n), dtype=np.float64, order="F")
+
+
+class Model:
+    """One wave field on one GPU: the module state of main_module.f90 plus a
+    device handle of libraytracer_gb300.so."""
+
+    def __init__(self, nx, ny, nz, nk, nl, nm, *, dt, f0=1e-4, sign_of_omega_i=1.0,
+                 enable_upper_reflection=True, enable_lower_reflection=True,
+                 precision="fp64", k_fixed=0.0, l_fixed=0.0, m_fixed=0.0):
+        self.n = (nx, ny, nz, nk, nl, nm)
+        self.dt = float(dt)
+        self.f0 = float(f0)
+        self.sign_of_omega_i = float(sign_of_omega_i)
+        self.enable_upper_reflection = bool(enable_upper_reflection)
+        self.enable_lower_reflection = bool(enable_lower_reflection)
+        self.precision = precision
+        self.fixed = (float(k_fixed), float(l_fixed), float(m_fixed))
+        self.itt = 0
+        # host arrays of allocate_main_module (main_module.f90:131-232)
+        self.E = zeros_padded(self.n)
+        n3 = self.n[:3]
+        self.Nsqr = zeros_padded(n3)
+        self.U = zeros_padded(n3)
+        self.V = zeros_padded(n3)
+        self.grid = None
+        self._lib = _lib.load()
+        dims = _lib.RtDims(nx, ny, nz, nk, nl, nm, ONX)
+        par = _lib.RtParams(self.dt, self.f0, self.sign_of_omega_i,
+                            int(self.enable_upper_reflection), int(self.enable_lower_reflection),
+                            PRECISIONS[precision])
+        h = ctypes.c_void_p()
+        rc = self._lib.rt_create(ctypes.byref(dims), ctypes.byref(par), ctypes.byref(h))
+        _lib.check(rc, None, "rt_create")
+        self._h = h
+        self._state_on_device = False
+
+    # ---- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc, what):
+        return _lib.check(rc, self._h, what)
+
+    # ---- setup (main.f90:36-47) ----------------------------------------------
+    def calc_grid(self, d_interior):
+        """set_grid + calc_grid: interior spacings -> padded grids."""
+        self.grid = calc_grid(self.n, d_interior, self.fixed)
+        for ax in AXES:  # xt, xu, dxt, dxu, ... as in main_module.f90:66-77
+            g = self.grid[ax]
+            setattr(self, ax + "t", g["t"])
+            setattr(self, ax + "u", g["u"])
+            setattr(self, "d" + ax + "t", g["dt"])
+            setattr(self, "d" + ax + "u", g["du"])
+        return self.grid
+
+    def coord(self, ax, key="t"):
+        return self.grid[ax][key]
+
+    def calc_parameter(self):
+        """calc_parameter (calc_parameter.f90:2-264) on the GPU."""
+        g = self.grid
+        arrs = [np.ascontiguousarray(g[ax]["dt"]) for ax in AXES]
+        arrs += [np.ascontiguousarray(g[ax]["t"]) for ax in ("k", "l", "m")]
+        self._check(self._lib.rt_set_grid(self._h, *[_lib.dptr(a) for a in arrs]), "rt_set_grid")
+        self._check(self._lib.rt_set_background(self._h, _lib.dptr(self.Nsqr), _lib.dptr(self.U),
+                                                _lib.dptr(self.V)), "rt_set_background")
+        self._check(self._lib.rt_calc_parameter(self._h), "rt_calc_parameter")
+
+    def max_rate(self):
+        r = ctypes.c_double()
+        self._check(self._lib.rt_max_rate(self._h, ctypes.byref(r)), "rt_max_rate")
+        return r.value
+
+    def set_dt(self, dt):
+        self.dt = float(dt)
+        self._check(self._lib.rt_set_dt(self._h, self.dt), "rt_set_dt")
+
+    def get_field(self, which):
+        out = zeros_padded(self.n)
+        self._check(self._lib.rt_get_field(self._h, which, _lib.dptr(out)), "rt_get_field")
+        return out
+
+    # ---- state ----------------------------------------------------------------
+    def set_state(self):
+        """Upload the host E (interior) to the device."""
+        self._check(self._lib.rt_set_state(self._h, _lib.dptr(self.E)), "rt_set_state")
+        self._state_on_device = True
+
+    def get_state(self):
+        """Download the device E into the host array (interior)."""
+        self._check(self._lib.rt_get_state(self._h, _lib.dptr(self.E)), "rt_get_state")
+        return self.E
+
+    # ---- time stepping (main.f90:64-79) ----------------------------------------
+    def integrate(self, nsteps=1):
+        """integrate (integrate.f90:4-271), nsteps times, state on the GPU."""
+        if not self._state_on_device:
+            self.set_state()
+        self._check(self._lib.rt_integrate(self._h, int(nsteps)), "rt_integrate")
+        self.itt += int(nsteps)
+
+    def integrate_host(self):
+        """One integrate on the host array (upload, step, download)."""
+        self._check(self._lib.rt_integrate_host(self._h, _lib.dptr(self.E)), "rt_integrate_host")
+        self._state_on_device = True
+        self.itt += 1
+
+    def diagnose(self, fields=True):
+        """Budget part of diagnose (diagnose.f90:46-329) for the last step.
+        Returns (budget dict, dict of padded 3D arrays or None)."""
+        b = _lib.RtBudget()
+        names = ("E_int", "meanfl_int", "diss_ks", "diss_ke", "diss_ls", "diss_le", "diss_ms", "diss_me")
+        arrs = {k: zeros_padded(self.n[:3]) for k in names} if fields else None
+        ptrs = [_lib.dptr(arrs[k]) if fields else None for k in names]
+        self._check(self._lib.rt_diagnose(self._h, ctypes.byref(b), *ptrs), "rt_diagnose")
+        return {k: getattr(b, k) for k in _lib.BUDGET_FIELDS}, arrs
+
+    # ---- plumbing ---------------------------------------------------------------
+    @property
+    def handle(self):
+        return self._h
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self._lib.rt_stream(self._h, ctypes.byref(s)), "rt_stream")
+        return s.value
+
+    def launch_count(self):
+        return int(self._lib.rt_launch_count(self._h))
+
+    def device_bytes(self):
+        return int(self._lib.rt_device_bytes(self._h))

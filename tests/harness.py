@@ -1,0 +1,52 @@
+"""Shared test helpers: build the oracle and the GPU model from one
+experiment description, and compare arrays on the ranges the path uses."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from oracle.oracle import Oracle  # noqa: E402
+from raytracer_3d_gb300 import configs  # noqa: E402
+from raytracer_3d_gb300.grid import ONX  # noqa: E402
+
+
+def build_oracle(exp, threads=False):
+    """The reference setup order (main.f90:36-47) on the oracle."""
+    o = Oracle(exp.n, threads=threads)
+    o.set_spacings(exp.d_interior)
+    dt0 = exp.dt if exp.dt else 1.0
+    o.set_scalars(dt0, exp.f0, exp.sign_of_omega_i, exp.upper, exp.lower, exp.fixed)
+    rc = o.calc_grid()
+    assert rc == 0, "oracle calc_grid check failed (%d)" % rc
+    exp.background(o)
+    exp.initial(o, np.random.Generator(np.random.PCG64(exp.seed)))
+    o.calc_parameter()
+    if exp.cfl is not None:
+        dt = exp.cfl / o.max_rate()
+        o.set_scalars(dt, exp.f0, exp.sign_of_omega_i, exp.upper, exp.lower, exp.fixed)
+        o.dt = dt
+    else:
+        o.dt = exp.dt
+    return o
+
+
+def interior(n):
+    return tuple(slice(ONX, ONX + k) for k in n)
+
+
+def face_range(n, a):
+    """faces 0..n along axis a, interior elsewhere (padded positions)."""
+    sl = list(interior(n))
+    sl[a] = slice(ONX - 1, ONX + n[a])
+    return tuple(sl)
+
+
+def max_rel(a, b):
+    """max |a-b| / max |b| (0 when both vanish)."""
+    den = float(np.max(np.abs(b)))
+    num = float(np.max(np.abs(a - b)))
+    return num / den if den > 0 else num

@@ -1,0 +1,191 @@
+"""Parity of the GPU path (through the C ABI) with the CPU oracle.
+
+The plain binary64 form reproduces the reference's arithmetic operation by
+operation, so coefficients, every state after every step and the
+wavenumber-integrated budget fields must be bit-identical; the scalar budget
+sums are reduced in a different order and must agree to 1e-12 relative.
+(The required tolerance for the FP64 form is 1e-12 relative L-infinity per
+step; the tests assert the stronger bit-identity and report it.)
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from harness import ONX, build_oracle, configs, face_range, interior, max_rel
+
+pytestmark = pytest.mark.gpu
+
+FP64_STEP_TOL = 1e-12   # relative L-inf per step (the stated bound)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+
+
+CASES = {
+    "shear_mini": lambda: configs.shear_mini(),
+    "shear_open": lambda: configs.shear_mini(upper=False, lower=False),
+    "shear_mixed_neg": lambda: configs.shear_mini(upper=True, lower=False, sign_of_omega_i=-1.0),
+    "ragged": lambda: configs.shear_mini(n=(7, 3, 5, 2, 6, 4)),
+    "min_n2": lambda: configs.shear_mini(n=(2, 2, 2, 2, 2, 2)),
+    "column_1d": lambda: configs.column_1d(fac=1),
+    "section_2d": lambda: configs.section_2d(fac=0.5),
+    "packet_small": lambda: configs.packet_small(),
+}
+
+VEL = ("xdot", "ydot", "zdot", "kdot", "ldot", "mdot")
+
+
+def _pair(name, precision="fp64"):
+    exp = CASES[name]()
+    m = configs.build_model(exp, precision)
+    o = build_oracle(exp)
+    return exp, m, o
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_coefficients_bit_identical(name):
+    exp, m, o = _pair(name)
+    from raytracer_3d_gb300 import _lib
+    try:
+        assert m.max_rate() == o.max_rate()
+        assert m.dt == o.dt
+        for a, v in enumerate(VEL):
+            got = m.get_field(a)
+            sl = face_range(exp.n, a)
+            ref = getattr(o, v)[sl]
+            assert np.array_equal(got[sl], ref), (v, max_rel(got[sl], ref))
+        sl = interior(exp.n)
+        for c, lam in enumerate(("lambda_x", "lambda_y", "lambda_z")):
+            got = m.get_field(_lib.RT_F_LAMBDA_X + c)
+            assert np.array_equal(got[sl], getattr(o, lam)[sl]), lam
+    finally:
+        m.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_steps_bit_identical(name):
+    exp, m, o = _pair(name)
+    sl = interior(exp.n)
+    try:
+        nsteps = 2 if name == "packet_small" else 4
+        for s in range(nsteps):
+            m.integrate(1)
+            o.integrate(1)
+            m.get_state()
+            rel = max_rel(m.E[sl], o.E[sl])
+            assert rel <= FP64_STEP_TOL, (s, rel)
+            assert np.array_equal(m.E[sl], o.E[sl]), (s, rel)
+    finally:
+        m.close()
+
+
+@pytest.mark.parametrize("name", ["shear_mini", "shear_open", "ragged", "section_2d", "column_1d"])
+def test_budget_matches_diagnose(name):
+    exp, m, o = _pair(name)
+    try:
+        m.integrate(2)
+        o.integrate(2)
+        b, f = m.diagnose()
+        bo = o.diagnose()
+        sl3 = interior(exp.n[:3])
+        for k in ("E_int", "meanfl_int", "diss_ks", "diss_ke", "diss_ls", "diss_le", "diss_ms", "diss_me"):
+            assert np.array_equal(f[k][sl3], getattr(o, k)[sl3]), k
+        for k in ("mfl_max", "umax", "vmax", "wmax", "kmax", "lmax", "mmax",
+                  "cfl_x", "cfl_y", "cfl_z", "cfl_k", "cfl_l", "cfl_m"):
+            assert b[k] == bo[k], (k, b[k], bo[k])
+        sums = [k for k in b if k in ("eint", "mflint") or k.startswith("bfl")]
+        scale = sum(abs(bo[k]) for k in sums) or 1.0
+        for k in sums:
+            assert abs(b[k] - bo[k]) <= 1e-12 * max(abs(bo[k]), 1e-300) + 1e-15 * scale, (k, b[k], bo[k])
+        assert abs(b["residual"]) <= 1e-12 * scale
+    finally:
+        m.close()
+
+
+def test_integrate_host_is_a_drop_in():
+    exp, m, o = _pair("shear_mini")
+    try:
+        ghost_before = m.E.copy()
+        m.integrate_host()
+        o.integrate(1)
+        sl = interior(exp.n)
+        assert np.array_equal(m.E[sl], o.E[sl])
+        mask = np.ones(m.E.shape, bool)
+        mask[sl] = False
+        assert np.array_equal(m.E[mask], ghost_before[mask])   # ghosts untouched
+    finally:
+        m.close()
+
+
+def test_call_order_errors():
+    from raytracer_3d_gb300 import Model, _lib
+    m = Model(4, 4, 4, 4, 4, 4, dt=1.0)
+    try:
+        with pytest.raises(_lib.RtError):
+            m._check(m._lib.rt_integrate(m.handle, 1), "rt_integrate")
+        b = _lib.RtBudget()
+        rc = m._lib.rt_diagnose(m.handle, ctypes.byref(b), *([None] * 8))
+        assert rc == -5
+    finally:
+        m.close()
+
+
+def test_launch_count_and_memory_are_reported():
+    exp, m, o = _pair("shear_mini")
+    try:
+        n0 = m.launch_count()
+        m.integrate(3)
+        assert m.launch_count() - n0 == 3
+        assert m.device_bytes() >= 2 * exp.cells * 8
+    finally:
+        m.close()
+
+
+def _energy(E, o, n):
+    vol = np.ones(n)
+    for a in range(6):
+        shp = [1] * 6
+        shp[a] = n[a]
+        vol = vol * o.grid["xyzklm"[a]]["dt"][ONX:ONX + n[a]].reshape(shp)
+    return float(np.sum(E * vol))
+
+
+def test_fp32_form_against_fp64_oracle():
+    """binary32 state/fluxes/velocities with binary64 coefficients: error
+    after 200 steps of the all-axes shear case."""
+    exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
+    m = configs.build_model(exp, "fp32")
+    o = build_oracle(exp)
+    sl = interior(exp.n)
+    try:
+        assert m.dt == o.dt
+        m.integrate(200)
+        o.integrate(200)
+        m.get_state()
+        ref = o.E[sl]
+        got = m.E[sl]
+        l2 = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        linf = max_rel(got, ref)
+        drift = abs(_energy(got, o, exp.n) - _energy(ref, o, exp.n)) / abs(_energy(ref, o, exp.n))
+        print("fp32 vs fp64 oracle after 200 steps: L2 %.3e Linf %.3e energy %.3e" % (l2, linf, drift))
+        assert l2 <= 1e-5
+        assert linf <= 1e-4
+        assert drift <= 1e-6
+    finally:
+        m.close()
+
+
+def test_fp32_budget_residual():
+    exp = configs.shear_mini()
+    m = configs.build_model(exp, "fp32")
+    try:
+        m.integrate(3)
+        b, f = m.diagnose()
+        scale = abs(b["eint"]) + abs(b["mflint"]) + sum(abs(b[k]) for k in b if k.startswith("bfl"))
+        assert abs(b["residual"]) <= 1e-5 * scale
+    finally:
+        m.close()
