@@ -176,12 +176,14 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-def run_form(precision, n, steps, warmup, dist, e2e_steps):
+def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None):
     import numpy as np
     import torch
     from raytracer_3d_gb300 import configs
     exp = configs.jet_large(n=n)
     m = configs.build_model(exp, precision)
+    if sched:
+        m.set_tuning(*sched)
     cells = exp.cells
     m.integrate(warmup)
     torch.cuda.synchronize()
@@ -222,10 +224,17 @@ def roofline(precision, cells, seconds_per_launch):
 def gpu_arm(args):
     rank, world, local, dist = dist_init(args.gpus)
     n = (args.n,) * 6
-    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps)
+    sched = (args.variant, args.band, args.threads)
+    if args.no_fp64:  # profiling runs of the fp32 form only
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched)
+        if rank == 0:
+            print(json.dumps({"profile_only": "fp32", "cells": f32["cells"],
+                              "ms_per_step": 1e3 * f32["seconds"] / args.steps}), flush=True)
+        return
+    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, sched)
     forms = {}
     if not args.no_fp32:
-        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0)
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched)
         forms["fp32"] = {"value": f32["cells"] * args.steps * world / f32["seconds"],
                          "ms_per_step": 1e3 * f32["seconds"] / args.steps,
                          "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
@@ -238,7 +247,7 @@ def gpu_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded log-normal spectrum, analytic N(z), U(y,z))",
         "config": {"workload": "jet_large %d^3x%d^3 plain fp64, CFL 0.4 (dt=%%.6g s)" % (n[0], n[0]) % main["dt"],
-                   "cells": cells, "form": "fp64", "l2": "state 8.6 GB per field >> L2; no flush needed",
+                   "cells": cells, "form": "fp64", "schedule": "%s band %d threads %d" % sched, "l2": "state 8.6 GB per field >> L2; no flush needed",
                    "parallelism": "replicas x%d" % world},
         "roofline": roofline("fp64", cells, main["seconds"] / args.steps),
         "clocks": main["clocks"],
@@ -286,6 +295,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
+    ap.add_argument("--variant", default="tma", choices=("tma", "plane", "cell"))
+    ap.add_argument("--band", type=int, default=8)
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the fp64 form (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

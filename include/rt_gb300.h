@@ -132,6 +132,20 @@ int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int,
                 double* diss_ke, double* diss_ls, double* diss_le, double* diss_ms,
                 double* diss_me);
 
+/* Schedule of the step kernel (no effect on results).  variant: 2 = plane
+ * tiled with bulk-copy (TMA) staging of the E planes (default; used when a
+ * plane of E is a multiple of 16 bytes), 0 = plane tiled with plain loads,
+ * 1 = one thread per cell; band: values per band of the plane schedule
+ * (default 8); threads: CTA size 128, 256 or 512.  Chosen by the autotuner
+ * (raytracer_3d_gb300.autotune). */
+int rt_set_tuning(rt_handle* h, int variant, int band, int threads);
+/* Sweep order of the plane schedule: 0 = bands over m (default), 1 = bands
+ * over l.  No effect on results. */
+int rt_set_schedule_sweep(rt_handle* h, int sweep);
+/* number of interior cells of the handle */
+long long rt_cells(const rt_handle* h);
+/* wait for the handle's stream; fails if a device-side wait timed out */
+int rt_sync(rt_handle* h);
 /* cudaStream_t of the handle (as void*), for timing with CUDA events */
 int rt_stream(rt_handle* h, void** stream);
 /* number of kernel launches issued by this handle so far */
@@ -140,6 +154,30 @@ long long rt_launch_count(const rt_handle* h);
 long long rt_device_bytes(const rt_handle* h);
 /* library version string */
 const char* rt_version(void);
+
+/* ---- batched ensemble -------------------------------------------------
+ * No counterpart in the reference, which advances one field per run: a
+ * batch advances many independent fields (members) of possibly different
+ * sizes with ONE persistent kernel launch per time step, replayed from
+ * captured CUDA graphs.  Members keep ownership of their state and
+ * coefficients; each keeps its own dt, grids and parameters.  All members
+ * must share one precision and have coefficients and a state.  Work queued
+ * on a member's own stream is ordered before the batch, and later member
+ * calls (rt_get_state, rt_diagnose, ...) after it.  Results are
+ * bit-identical to stepping each member alone. */
+typedef struct rt_batch rt_batch;
+int rt_batch_create(rt_handle* const* members, int n, rt_batch** out);
+int rt_batch_destroy(rt_batch* b);
+const char* rt_batch_last_error(const rt_batch* b);
+/* band, CTA size (128/256/512), sweep order (0/1) and steps per captured
+ * graph (even); chosen by the autotuner (raytracer_3d_gb300.autotune) */
+int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps);
+/* advance every member by nsteps (asynchronous on the batch stream) */
+int rt_batch_integrate(rt_batch* b, int nsteps);
+int rt_batch_sync(rt_batch* b);
+int rt_batch_stream(rt_batch* b, void** stream);
+long long rt_batch_launch_count(const rt_batch* b);
+long long rt_batch_cells(const rt_batch* b);
 
 #ifdef __cplusplus
 }

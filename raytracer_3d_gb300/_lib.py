@@ -58,10 +58,23 @@ SIGNATURES = {
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_integrate_host": (ctypes.c_int, [_P, _D]),
     "rt_diagnose": (ctypes.c_int, [_P, ctypes.POINTER(RtBudget)] + [_D] * 8),
+    "rt_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "rt_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "rt_launch_count": (ctypes.c_longlong, [_P]),
     "rt_device_bytes": (ctypes.c_longlong, [_P]),
     "rt_version": (ctypes.c_char_p, []),
+    "rt_set_schedule_sweep": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_sync": (ctypes.c_int, [_P]),
+    "rt_cells": (ctypes.c_longlong, [_P]),
+    "rt_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(_P)]),
+    "rt_batch_destroy": (ctypes.c_int, [_P]),
+    "rt_batch_last_error": (ctypes.c_char_p, [_P]),
+    "rt_batch_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "rt_batch_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_batch_sync": (ctypes.c_int, [_P]),
+    "rt_batch_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "rt_batch_launch_count": (ctypes.c_longlong, [_P]),
+    "rt_batch_cells": (ctypes.c_longlong, [_P]),
 }
 
 _lib = None

@@ -23,6 +23,8 @@
 #include "rt_coeff.cuh"
 #include "rt_kernels.h"
 #include "rt_step.cuh"
+#include "rt_step2.cuh"
+#include "rt_step3.cuh"
 
 using namespace rt;
 
@@ -46,12 +48,15 @@ struct rt_handle {
   long long scratch_len = 0;
   double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
   double* result = nullptr;     // DIAG_RESULT_NV doubles
+  int* status = nullptr;        // device flag raised by a timed-out wait
   void* pinned = nullptr;       // host staging of one interior field
   double rate = 0.0;
+  StepTuning tune;
   bool have_grid = false, have_bg = false, have_coeff = false, have_state = false;
   long long steps_since_set = 0;
   long long launches = 0;
   long long bytes = 0;
+  cudaEvent_t ev = nullptr;     // orders this handle's stream against a batch stream
   std::string err;
 };
 
@@ -183,6 +188,7 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   A.E = (const T*)h->E[src];
   A.Enew = (T*)h->E[1 - src];
   A.dt = h->p.dt;
+  A.status = h->status;
   return A;
 }
 
@@ -201,10 +207,253 @@ static int upload_tab32(rt_handle* h) {
   return RT_OK;
 }
 
+// after a synchronisation: report a device-side wait that timed out
+static int check_status(rt_handle* h) {
+  int st = 0;
+  CUDA_TRY(h, cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) return fail(h, RT_ERR_CUDA, "a device-side wait timed out (status %d); results are invalid", st);
+  return RT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched ensemble
+// ---------------------------------------------------------------------------
+struct rt_batch {
+  std::vector<rt_handle*> mem;
+  std::vector<int> cur0;        // members' ping-pong index when the arrays were built
+  int fp64 = 0;
+  int parity = 0;               // steps taken since the arrays were built, mod 2
+  cudaStream_t st = nullptr;
+  void* d_mem[2] = {nullptr, nullptr};   // BatchMember<T> arrays for the two parities
+  long long* d_first = nullptr;
+  size_t smem = 0;
+  bool tma = false;
+  StepTuning tune;
+  int grid = 0;
+  int graph_steps = 16;         // steps per captured graph (even)
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // graphs starting at parity 0 / 1
+  bool dirty = true;
+  long long launches = 0;
+  long long cells = 0;
+  cudaEvent_t ev = nullptr;
+  std::string err;
+};
+
+static int bfail(rt_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf; else g_create_err = buf;
+  return code;
+}
+
+#define BCUDA_TRY(b, call)                                                             \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return bfail(b, RT_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),    \
+                   __FILE__, __LINE__);                                                \
+  } while (0)
+
+static void batch_free_graphs(rt_batch* b) {
+  for (int k = 0; k < 2; k++)
+    if (b->gexec[k]) { cudaGraphExecDestroy(b->gexec[k]); b->gexec[k] = nullptr; }
+}
+
+template <class T>
+static cudaError_t batch_launch(rt_batch* b, const void* mem) {
+  const int n = (int)b->mem.size();
+  if (b->tma) return launch_batch_tma<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
+  return launch_batch<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
+}
+
+template <class T>
+static int batch_build(rt_batch* b) {
+  const int n = (int)b->mem.size();
+  std::vector<BatchMember<T>> arr[2];
+  std::vector<long long> first(n + 1, 0);
+  size_t smem = 0;
+  bool tma = true;
+  for (int j = 0; j < n; j++) tma = tma && tma_path_ok<T>(b->mem[j]->d);
+  for (int j = 0; j < n; j++) {
+    rt_handle* h = b->mem[j];
+    StepTuning tn = b->tune;
+    for (int par = 0; par < 2; par++) {
+      BatchMember<T> bm;
+      bm.A = make_step_args<T>(h, par == 0 ? h->cur : 1 - h->cur);
+      bm.S = make_sched(h->d, tn);
+      arr[par].push_back(bm);
+    }
+    first[j + 1] = first[j] + sched_items(h->d, arr[0].back().S);
+    smem = std::max(smem, tma ? tma_path_smem<T>(h->d) : plane_smem<T>(h->d));
+    b->cur0[j] = h->cur;
+  }
+  for (int par = 0; par < 2; par++) {
+    if (!b->d_mem[par]) BCUDA_TRY(b, cudaMalloc(&b->d_mem[par], (size_t)n * sizeof(BatchMember<T>)));
+    BCUDA_TRY(b, cudaMemcpy(b->d_mem[par], arr[par].data(), (size_t)n * sizeof(BatchMember<T>),
+                            cudaMemcpyHostToDevice));
+  }
+  if (!b->d_first) BCUDA_TRY(b, cudaMalloc(&b->d_first, (size_t)(n + 1) * sizeof(long long)));
+  BCUDA_TRY(b, cudaMemcpy(b->d_first, first.data(), (size_t)(n + 1) * sizeof(long long),
+                          cudaMemcpyHostToDevice));
+  b->smem = smem;
+  b->tma = tma;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int per_sm = batch_blocks_per_sm<T>(b->tune.threads, smem, tma);
+  if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batch kernel does not fit on an SM");
+  const long long items = first[n];
+  b->grid = (int)std::min<long long>(items, (long long)per_sm * nsm);
+  b->parity = 0;
+  // capture graph_steps launches starting at each parity
+  batch_free_graphs(b);
+  for (int start = 0; start < 2; start++) {
+    cudaGraph_t g;
+    BCUDA_TRY(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int t = 0; t < b->graph_steps && e == cudaSuccess; t++)
+      e = batch_launch<T>(b, b->d_mem[(start + t) & 1]);
+    cudaError_t e2 = cudaStreamEndCapture(b->st, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess)
+      return bfail(b, RT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    e = cudaGraphInstantiate(&b->gexec[start], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  b->dirty = false;
+  return RT_OK;
+}
+
+template <class T>
+static int batch_run(rt_batch* b, int nsteps) {
+  const int n = (int)b->mem.size();
+  for (int j = 0; j < n; j++)  // a member stepped on its own since the build
+    if (b->mem[j]->cur != (b->cur0[j] ^ b->parity)) b->dirty = true;
+  // the batch stream runs after everything queued on the members' streams
+  for (int j = 0; j < n; j++) {
+    BCUDA_TRY(b, cudaEventRecord(b->mem[j]->ev, b->mem[j]->st));
+    BCUDA_TRY(b, cudaStreamWaitEvent(b->st, b->mem[j]->ev, 0));
+  }
+  if (b->dirty) {
+    int rc = batch_build<T>(b);
+    if (rc) return rc;
+  }
+  int left = nsteps;
+  while (left >= b->graph_steps) {
+    BCUDA_TRY(b, cudaGraphLaunch(b->gexec[b->parity], b->st));
+    b->launches += b->graph_steps;
+    left -= b->graph_steps;  // graph_steps is even: parity unchanged
+  }
+  while (left > 0) {
+    cudaError_t e = batch_launch<T>(b, b->d_mem[b->parity]);
+    if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
+    b->launches += 1;
+    b->parity ^= 1;
+    left -= 1;
+  }
+  // and later work on a member's own stream runs after the batch
+  BCUDA_TRY(b, cudaEventRecord(b->ev, b->st));
+  for (int j = 0; j < n; j++) {
+    rt_handle* h = b->mem[j];
+    BCUDA_TRY(b, cudaStreamWaitEvent(h->st, b->ev, 0));
+    h->cur = b->cur0[j] ^ b->parity;
+    h->steps_since_set += nsteps;
+  }
+  return RT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
+
+int rt_batch_create(rt_handle* const* members, int n, rt_batch** out) {
+  if (!members || n < 1 || !out) return bfail(nullptr, RT_ERR_ARG, "rt_batch_create: no members");
+  *out = nullptr;
+  const int prec = members[0]->p.precision;
+  for (int j = 0; j < n; j++) {
+    rt_handle* h = members[j];
+    if (!h) return bfail(nullptr, RT_ERR_ARG, "rt_batch_create: member %d is NULL", j);
+    if (h->p.precision != prec) return bfail(nullptr, RT_ERR_ARG, "rt_batch_create: mixed precisions");
+    if (!h->have_coeff || !h->have_state)
+      return bfail(nullptr, RT_ERR_STATE, "rt_batch_create: member %d needs rt_calc_parameter and rt_set_state", j);
+    const bool ok = prec == RT_FP64 ? plane_ok<double>(h->d) : plane_ok<float>(h->d);
+    if (!ok) return bfail(nullptr, RT_ERR_ARG, "rt_batch_create: member %d plane nx*ny too large", j);
+    for (int k = 0; k < j; k++)
+      if (members[k] == h) return bfail(nullptr, RT_ERR_ARG, "rt_batch_create: member %d repeated", j);
+  }
+  rt_batch* b = new rt_batch();
+  b->mem.assign(members, members + n);
+  b->cur0.assign(n, 0);
+  b->fp64 = prec == RT_FP64;
+  for (int j = 0; j < n; j++) b->cells += members[j]->d.ncell;
+  if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess) {
+    delete b;
+    return bfail(nullptr, RT_ERR_CUDA, "rt_batch_create: stream creation failed");
+  }
+  // members' own streams may still run setup work: order it before the batch
+  for (int j = 0; j < n; j++) cudaStreamSynchronize(members[j]->st);
+  *out = b;
+  return RT_OK;
+}
+
+int rt_batch_destroy(rt_batch* b) {
+  if (!b) return RT_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  batch_free_graphs(b);
+  for (int k = 0; k < 2; k++) cudaFree(b->d_mem[k]);
+  cudaFree(b->d_first);
+  if (b->ev) cudaEventDestroy(b->ev);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return RT_OK;
+}
+
+const char* rt_batch_last_error(const rt_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }
+
+int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps) {
+  if (!b) return RT_ERR_ARG;
+  if (band < 1 || band > 1024) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: band %d out of range", band);
+  if (threads != 128 && threads != 256 && threads != 512)
+    return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: threads must be 128, 256 or 512");
+  if (sweep != 0 && sweep != 1) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: sweep must be 0 or 1");
+  if (graph_steps < 2 || graph_steps % 2) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: graph_steps must be even and >= 2");
+  cudaStreamSynchronize(b->st);
+  b->tune.band = band;
+  b->tune.threads = threads;
+  b->tune.sweep = sweep;
+  b->graph_steps = graph_steps;
+  b->dirty = true;
+  return RT_OK;
+}
+
+int rt_batch_integrate(rt_batch* b, int nsteps) {
+  if (!b) return RT_ERR_ARG;
+  if (nsteps < 0) return bfail(b, RT_ERR_ARG, "rt_batch_integrate: nsteps < 0");
+  return b->fp64 ? batch_run<double>(b, nsteps) : batch_run<float>(b, nsteps);
+}
+
+int rt_batch_sync(rt_batch* b) {
+  if (!b) return RT_ERR_ARG;
+  BCUDA_TRY(b, cudaStreamSynchronize(b->st));
+  for (rt_handle* h : b->mem)
+    if (check_status(h)) return bfail(b, RT_ERR_CUDA, "member: %s", h->err.c_str());
+  return RT_OK;
+}
+
+int rt_batch_stream(rt_batch* b, void** stream) {
+  if (!b || !stream) return RT_ERR_ARG;
+  *stream = (void*)b->st;
+  return RT_OK;
+}
+
+long long rt_batch_launch_count(const rt_batch* b) { return b ? b->launches : 0; }
+long long rt_batch_cells(const rt_batch* b) { return b ? b->cells : 0; }
+
 
 const char* rt_version(void) { return "raytracer_gb300 0.1 (sm_103a)"; }
 
@@ -259,7 +508,8 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
     rt_destroy(h);
     return code;
   };
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(h, RT_ERR_CUDA, "rt_create: stream creation failed"));
 
   long long gl = 0;
@@ -287,6 +537,8 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
   if ((rc = dev_alloc(h, (void**)&h->scratch, h->scratch_len * sizeof(double)))) return bail(rc);
   if ((rc = dev_alloc(h, (void**)&h->vol3, 8 * d.nvol3 * sizeof(double)))) return bail(rc);
   if ((rc = dev_alloc(h, (void**)&h->result, 32 * sizeof(double)))) return bail(rc);
+  if ((rc = dev_alloc(h, (void**)&h->status, sizeof(int)))) return bail(rc);
+  if (cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess) return bail(fail(h, RT_ERR_CUDA, "memset"));
   *out = h;
   return RT_OK;
 }
@@ -303,7 +555,9 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->scratch);
   cudaFree(h->vol3);
   cudaFree(h->result);
+  cudaFree(h->status);
   if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->ev) cudaEventDestroy(h->ev);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return RT_OK;
@@ -513,6 +767,7 @@ int rt_get_state(rt_handle* h, double* E) {
   const Dims& d = h->d;
   CUDA_TRY(h, cudaMemcpyAsync(h->pinned, h->E[h->cur], (size_t)d.ncell * h->elem, cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  if ((rc = check_status(h))) return rc;
   if (h->p.precision == RT_FP64) scatter_interior<double>(d, (const double*)h->pinned, E);
   else scatter_interior<float>(d, (const float*)h->pinned, E);
   return RT_OK;
@@ -525,8 +780,8 @@ int rt_integrate(rt_handle* h, int nsteps) {
   if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_integrate: rt_set_state first");
   for (int t = 0; t < nsteps; t++) {
     cudaError_t e;
-    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->st);
-    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->st);
+    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->tune, h->st);
+    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->tune, h->st);
     h->launches += 1;
     if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     h->cur = 1 - h->cur;
@@ -564,6 +819,10 @@ int rt_diagnose(rt_handle* h, rt_budget* o, double* E_int, double* meanfl_int, d
   std::vector<double> v3((size_t)8 * d.nvol3);
   CUDA_TRY(h, cudaMemcpyAsync(v3.data(), h->vol3, v3.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  {
+    int rc = check_status(h);
+    if (rc) return rc;
+  }
   o->eint = r[0]; o->mflint = r[1]; o->mfl_max = r[2];
   o->umax = r[3]; o->vmax = r[4]; o->wmax = r[5]; o->kmax = r[6]; o->lmax = r[7]; o->mmax = r[8];
   double* b = &o->bfl_xs;
@@ -596,6 +855,32 @@ int rt_diagnose(rt_handle* h, rt_budget* o, double* E_int, double* meanfl_int, d
   return RT_OK;
 }
 
+int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
+  if (!h) return RT_ERR_ARG;
+  if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA)
+    return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
+  if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
+  if (threads != 128 && threads != 256 && threads != 512)
+    return fail(h, RT_ERR_ARG, "rt_set_tuning: threads must be 128, 256 or 512");
+  h->tune.variant = variant;
+  h->tune.band = band;
+  h->tune.threads = threads;
+  return RT_OK;
+}
+
+int rt_set_schedule_sweep(rt_handle* h, int sweep) {
+  if (!h) return RT_ERR_ARG;
+  if (sweep != 0 && sweep != 1) return fail(h, RT_ERR_ARG, "rt_set_schedule_sweep: sweep must be 0 or 1");
+  h->tune.sweep = sweep;
+  return RT_OK;
+}
+
+int rt_sync(rt_handle* h) {
+  if (!h) return RT_ERR_ARG;
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  return check_status(h);
+}
+
 int rt_stream(rt_handle* h, void** stream) {
   if (!h || !stream) return RT_ERR_ARG;
   *stream = (void*)h->st;
@@ -603,6 +888,7 @@ int rt_stream(rt_handle* h, void** stream) {
 }
 
 long long rt_launch_count(const rt_handle* h) { return h ? h->launches : 0; }
+long long rt_cells(const rt_handle* h) { return h ? h->d.ncell : 0; }
 long long rt_device_bytes(const rt_handle* h) { return h ? h->bytes : 0; }
 
 }  // extern "C"

@@ -6,6 +6,8 @@
 
 #include "rt_coeff.cuh"
 #include "rt_step.cuh"
+#include "rt_step2.cuh"
+#include "rt_step3.cuh"
 
 namespace rt {
 
@@ -491,13 +493,140 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
   return cudaGetLastError();
 }
 
+PlaneSched make_sched(const Dims& d, const StepTuning& tn) {
+  PlaneSched S;
+  S.sweep = tn.sweep ? 1 : 0;
+  const int nb = S.sweep ? d.n[4] : d.n[5];
+  S.band = tn.band > 0 ? tn.band : 8;
+  if (S.band > nb) S.band = nb;
+  S.nband = (nb + S.band - 1) / S.band;
+  S.nunits = (long long)d.n[2] * d.n[3];
+  return S;
+}
+
+long long sched_items(const Dims& d, const PlaneSched& S) {
+  const int nouter = S.sweep ? d.n[5] : d.n[4];
+  return (long long)S.nband * nouter * S.band * S.nunits;
+}
+
 template <class T>
-cudaError_t launch_step(const StepArgs<T>& A, cudaStream_t st) {
+size_t plane_smem(const Dims& d) { return (size_t)3 * d.n[0] * d.n[1] * sizeof(T); }
+
+template <class T>
+bool plane_ok(const Dims& d) { return plane_smem<T>(d) <= 48 * 1024; }
+template size_t plane_smem<double>(const Dims&);
+template size_t plane_smem<float>(const Dims&);
+template bool plane_ok<double>(const Dims&);
+template bool plane_ok<float>(const Dims&);
+
+template <class T>
+bool tma_path_ok(const Dims& d) { return tma_ok<T>(d) && tma_smem<T>(d) <= 200 * 1024; }
+template <class T>
+size_t tma_path_smem(const Dims& d) { return tma_smem<T>(d); }
+template bool tma_path_ok<double>(const Dims&);
+template bool tma_path_ok<float>(const Dims&);
+template size_t tma_path_smem<double>(const Dims&);
+template size_t tma_path_smem<float>(const Dims&);
+
+template <class T, int NT, class K>
+static cudaError_t set_smem(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class T, int NT>
+static cudaError_t launch_tma_nt(const StepArgs<T>& A, const PlaneSched& S, long long nblk,
+                                 cudaStream_t st) {
+  const size_t sm = tma_smem<T>(A.d);
+  cudaError_t e = set_smem<T, NT>(step_tma_kernel<T, NT>, sm);
+  if (e != cudaSuccess) return e;
+  step_tma_kernel<T, NT><<<(unsigned)nblk, NT, sm, st>>>(A, S);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st) {
+  if (tn.variant == RT_VARIANT_TMA && tma_path_ok<T>(A.d)) {
+    const PlaneSched S = make_sched(A.d, tn);
+    const long long nblk = sched_items(A.d, S);
+    if (tn.threads == 128) return launch_tma_nt<T, 128>(A, S, nblk, st);
+    if (tn.threads == 512) return launch_tma_nt<T, 512>(A, S, nblk, st);
+    return launch_tma_nt<T, 256>(A, S, nblk, st);
+  }
+  if ((tn.variant == RT_VARIANT_PLANE || tn.variant == RT_VARIANT_TMA) && plane_ok<T>(A.d)) {
+    const PlaneSched S = make_sched(A.d, tn);
+    const long long nblk = sched_items(A.d, S);
+    const size_t sm = plane_smem<T>(A.d);
+    if (tn.threads == 128)
+      step_plane_kernel<T, 128><<<(unsigned)nblk, 128, sm, st>>>(A, S);
+    else if (tn.threads == 512)
+      step_plane_kernel<T, 512><<<(unsigned)nblk, 512, sm, st>>>(A, S);
+    else
+      step_plane_kernel<T, 256><<<(unsigned)nblk, 256, sm, st>>>(A, S);
+    return cudaGetLastError();
+  }
   step_kernel<T><<<cell_grid(A.d, 256), 256, 0, st>>>(A);
   return cudaGetLastError();
 }
-template cudaError_t launch_step<double>(const StepArgs<double>&, cudaStream_t);
-template cudaError_t launch_step<float>(const StepArgs<float>&, cudaStream_t);
+template cudaError_t launch_step<double>(const StepArgs<double>&, const StepTuning&, cudaStream_t);
+template cudaError_t launch_step<float>(const StepArgs<float>&, const StepTuning&, cudaStream_t);
+
+template <class T>
+cudaError_t launch_batch(const void* members, const long long* first, int nmem, size_t smem,
+                         int threads, int grid, cudaStream_t st) {
+  const BatchMember<T>* mem = (const BatchMember<T>*)members;
+  if (threads == 128)
+    batch_plane_kernel<T, 128><<<grid, 128, smem, st>>>(mem, first, nmem);
+  else if (threads == 512)
+    batch_plane_kernel<T, 512><<<grid, 512, smem, st>>>(mem, first, nmem);
+  else
+    batch_plane_kernel<T, 256><<<grid, 256, smem, st>>>(mem, first, nmem);
+  return cudaGetLastError();
+}
+template cudaError_t launch_batch<double>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+template cudaError_t launch_batch<float>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+
+template <class T, int NT>
+static int occ_batch(bool tma, size_t smem) {
+  int nb = 0;
+  cudaError_t e;
+  if (tma) {
+    e = set_smem<T, NT>(batch_tma_kernel<T, NT>, smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_tma_kernel<T, NT>, NT, smem);
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_plane_kernel<T, NT>, NT, smem);
+  }
+  if (e != cudaSuccess) { cudaGetLastError(); return 0; }
+  return nb;
+}
+
+template <class T>
+int batch_blocks_per_sm(int threads, size_t smem, bool tma) {
+  if (threads == 128) return occ_batch<T, 128>(tma, smem);
+  if (threads == 512) return occ_batch<T, 512>(tma, smem);
+  return occ_batch<T, 256>(tma, smem);
+}
+template int batch_blocks_per_sm<double>(int, size_t, bool);
+template int batch_blocks_per_sm<float>(int, size_t, bool);
+
+template <class T>
+cudaError_t launch_batch_tma(const void* members, const long long* first, int nmem, size_t smem,
+                             int threads, int grid, cudaStream_t st) {
+  const BatchMember<T>* mem = (const BatchMember<T>*)members;
+  if (threads == 128)
+    batch_tma_kernel<T, 128><<<grid, 128, smem, st>>>(mem, first, nmem);
+  else if (threads == 512)
+    batch_tma_kernel<T, 512><<<grid, 512, smem, st>>>(mem, first, nmem);
+  else
+    batch_tma_kernel<T, 256><<<grid, 256, smem, st>>>(mem, first, nmem);
+  return cudaGetLastError();
+}
+template cudaError_t launch_batch_tma<double>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+template cudaError_t launch_batch_tma<float>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+
+size_t batch_member_bytes(int precision_fp64) {
+  return precision_fp64 ? sizeof(BatchMember<double>) : sizeof(BatchMember<float>);
+}
 
 DiagSizes diag_sizes(const Dims& d) {
   DiagSizes s;

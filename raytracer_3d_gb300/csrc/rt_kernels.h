@@ -47,8 +47,41 @@ cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf
 cudaError_t launch_to_fp32(const double* src, float* dst, long long n, cudaStream_t st);
 cudaError_t launch_lam_combine(const double* lx, const double* ly, const double* lz, int ux, int uy,
                                int uz, float* dst, long long n, cudaStream_t st);
+// step kernel variants: the plane-tiled kernel (rt_step2.cuh) and the
+// one-thread-per-cell kernel (rt_step.cuh), kept as the fallback for planes
+// that do not fit in shared memory
+#define RT_VARIANT_PLANE 0
+#define RT_VARIANT_CELL 1
+#define RT_VARIANT_TMA 2
+struct StepTuning {
+  int variant = RT_VARIANT_TMA;
+  int band = 8;       // values per band of the plane schedule
+  int threads = 256;  // CTA size of the plane kernel (128, 256, 512)
+  int sweep = 0;      // 0: bands over m, 1: bands over l
+};
+struct PlaneSched;
+PlaneSched make_sched(const Dims& d, const StepTuning& tn);
+long long sched_items(const Dims& d, const PlaneSched& S);
 template <class T>
-cudaError_t launch_step(const StepArgs<T>& A, cudaStream_t st);
+bool plane_ok(const Dims& d);
+template <class T>
+size_t plane_smem(const Dims& d);
+// batched ensemble (members: device array of BatchMember<T>)
+template <class T>
+cudaError_t launch_batch(const void* members, const long long* first, int nmem, size_t smem,
+                         int threads, int grid, cudaStream_t st);
+template <class T>
+int batch_blocks_per_sm(int threads, size_t smem, bool tma);
+template <class T>
+bool tma_path_ok(const Dims& d);
+template <class T>
+size_t tma_path_smem(const Dims& d);
+template <class T>
+cudaError_t launch_batch_tma(const void* members, const long long* first, int nmem, size_t smem,
+                             int threads, int grid, cudaStream_t st);
+size_t batch_member_bytes(int precision_fp64);
+template <class T>
+cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st);
 DiagSizes diag_sizes(const Dims& d);
 template <class T>
 cudaError_t launch_diag(const StepArgs<T>& A, const T* Ecur, double* scratch, double* vol3,

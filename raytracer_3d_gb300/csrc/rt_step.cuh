@@ -65,6 +65,7 @@ struct StepArgs {
   const T* vlo[6];     // face-0 planes
   const T* lam[3];     // fp64: lambda_x/y/z; fp32: lam[0] = combined rate
   double dt;
+  int* status;         // device flag: bit 0 = a bounded wait timed out
 };
 
 // Read E at cell p displaced by off along axis a from coordinate c,

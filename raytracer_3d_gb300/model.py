@@ -162,6 +162,17 @@ class Model:
         return {k: getattr(b, k) for k in _lib.BUDGET_FIELDS}, arrs
 
     # ---- plumbing ---------------------------------------------------------------
+    VARIANTS = {"plane": 0, "cell": 1, "tma": 2}
+
+    def set_tuning(self, variant="tma", band=8, threads=256, sweep=0):
+        """Schedule of the step kernel; never changes results."""
+        self._check(self._lib.rt_set_tuning(self._h, self.VARIANTS[variant], int(band), int(threads)),
+                    "rt_set_tuning")
+        self._check(self._lib.rt_set_schedule_sweep(self._h, int(sweep)), "rt_set_schedule_sweep")
+
+    def sync(self):
+        self._check(self._lib.rt_sync(self._h), "rt_sync")
+
     @property
     def handle(self):
         return self._h

@@ -1,0 +1,70 @@
+"""Batched ensemble: one persistent launch per step over members of
+different sizes gives each member exactly the result it gets alone."""
+import numpy as np
+import pytest
+
+from harness import configs, interior
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+
+
+def _members(count, seed, steps=7, spatial=(4, 6, 8), spectral=(4, 6, 8)):
+    rng = np.random.default_rng(seed)
+    return [configs.ensemble_member(rng, steps=steps, spatial=spatial, spectral=spectral) for _ in range(count)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("tuning", [(8, 256, 0, 16), (3, 128, 1, 2), (1, 512, 0, 4)])
+def test_batch_equals_members_alone(precision, tuning):
+    from raytracer_3d_gb300.batch import Batch
+    exps = _members(6, seed=11)
+    alone = []
+    for e in exps:
+        m = configs.build_model(e, precision)
+        m.integrate(e.steps)
+        alone.append(m.get_state().copy())
+        m.close()
+    models = [configs.build_model(e, precision) for e in exps]
+    b = Batch(models)
+    b.set_tuning(*tuning)
+    b.integrate(3)
+    b.integrate(4)          # 7 steps: graphs and single launches, both parities
+    for e, m, ref in zip(exps, models, alone):
+        got = m.get_state()
+        sl = interior(e.n)
+        assert np.array_equal(got[sl], ref[sl]), e.n
+    assert b.launch_count() == 7
+    b.close()
+    for m in models:
+        m.close()
+
+
+def test_member_can_leave_and_step_alone():
+    from raytracer_3d_gb300.batch import Batch
+    exps = _members(3, seed=5)
+    ref = []
+    for e in exps:
+        m = configs.build_model(e, "fp32")
+        m.integrate(5)
+        ref.append(m.get_state().copy())
+        m.close()
+    models = [configs.build_model(e, "fp32") for e in exps]
+    b = Batch(models)
+    b.integrate(2)
+    models[1].integrate(1)   # one member steps on its own stream between batch calls
+    b2 = Batch([models[0], models[2]])
+    b2.integrate(3)
+    models[1].integrate(2)
+    for e, m, r in zip(exps, models, ref):
+        sl = interior(e.n)
+        assert np.array_equal(m.get_state()[sl], r[sl])
+    b.close()
+    b2.close()
+    for m in models:
+        m.close()

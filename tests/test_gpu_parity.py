@@ -66,9 +66,15 @@ def test_coefficients_bit_identical(name):
         m.close()
 
 
+SCHEDULES = [("tma", 8, 256, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plane", 8, 256, 0),
+             ("plane", 2, 512, 1), ("cell", 8, 256, 0)]
+
+
 @pytest.mark.parametrize("name", list(CASES))
-def test_steps_bit_identical(name):
+@pytest.mark.parametrize("sched", SCHEDULES, ids=lambda s: "%s-b%d-t%d-s%d" % s)
+def test_steps_bit_identical(name, sched):
     exp, m, o = _pair(name)
+    m.set_tuning(*sched)
     sl = interior(exp.n)
     try:
         nsteps = 2 if name == "packet_small" else 4
@@ -154,11 +160,29 @@ def _energy(E, o, n):
     return float(np.sum(E * vol))
 
 
-def test_fp32_form_against_fp64_oracle():
+def test_fp32_schedules_agree():
+    """the schedule never changes the binary32 result"""
+    exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
+    outs = []
+    for sched in SCHEDULES:
+        m = configs.build_model(exp, "fp32")
+        m.set_tuning(*sched)
+        m.integrate(5)
+        outs.append(m.get_state().copy())
+        m.close()
+    for o in outs[1:5]:
+        assert np.array_equal(o, outs[0])
+    # the cell kernel may contract multiply-adds differently
+    assert max_rel(outs[5], outs[0]) < 1e-6
+
+
+@pytest.mark.parametrize("variant", ["tma", "plane", "cell"])
+def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
     after 200 steps of the all-axes shear case."""
     exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
     m = configs.build_model(exp, "fp32")
+    m.set_tuning(variant)
     o = build_oracle(exp)
     sl = interior(exp.n)
     try:
