@@ -210,6 +210,76 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None):
     return out
 
 
+def bench_batched(steps, warmup, members=48, seed=2024):
+    """48 independent fp32 instances (dims per axis from {8,16,24,32} spatial
+    and {8,12,16,24} spectral, own N0, f, mean-flow amplitude, packet init)
+    advanced by one persistent, graph-captured launch per step, with the
+    schedule chosen by the autotuner."""
+    import numpy as np
+    import torch
+    from raytracer_3d_gb300 import configs
+    from raytracer_3d_gb300.autotune import tune_batch
+    from raytracer_3d_gb300.batch import Batch
+    rng = np.random.default_rng(seed)
+    exps = [configs.ensemble_member(rng, steps=500) for _ in range(members)]
+    t0 = time.perf_counter()
+    models = []
+    for e in exps:
+        m = configs.build_model(e, "fp32")
+        m.E = None          # the host copy is not needed for the timing
+        models.append(m)
+    setup_s = time.perf_counter() - t0
+    b = Batch(models)
+    best, table = tune_batch(b, reps=2, use_cache=False)
+    b.integrate(warmup)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = b.launch_count()
+    with ClockSampler(torch.cuda.current_device()) as cs:
+        e0.record(stream)
+        b.integrate(steps)
+        e1.record(stream)
+        e1.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3
+    b.sync()
+    cells = b.cells
+    out = {"value": cells * steps / secs, "unit": UNIT, "members": members, "cells_per_step": cells,
+           "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": b.launch_count() - l0,
+           "graph_steps": b.tuning[3], "tuning": {"band": best[0], "threads": best[1], "sweep": best[2]},
+           "roofline": roofline("fp32", cells, secs / steps), "clocks": cs.summary(),
+           "setup_s": round(setup_s, 2)}
+    b.close()
+    for m in models:
+        m.close()
+    return out
+
+
+def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
+    """Poisson arrivals (mean 20/s), step counts uniform in [50,1000], dims
+    as the batched form, 120 GB HBM budget, fp32 continuous batching; and the
+    fp64 one-at-a-time baseline on the first requests."""
+    from raytracer_3d_gb300.serve import GpuExecutor, SequentialExecutor, Server, poisson_requests
+    reqs = poisson_requests(nreq, rate=rate, seed=seed)
+    ex = GpuExecutor("fp32", batch_tuning=(8, 256, 0, 16))
+    rep = Server(ex, budget_bytes=budget, chunk_max=50).run(reqs)
+    ex.close()
+    s = rep.summary()
+    for r in reqs:
+        r.result = None
+    base = poisson_requests(baseline_req, rate=rate, seed=seed)
+    exb = SequentialExecutor("fp64")
+    repb = Server(exb, budget_bytes=budget, chunk_max=10 ** 9, max_members=1).run(base)
+    sb = repb.summary()
+    return {"requests": nreq, "arrival_rate_per_s": rate, "budget_bytes": budget,
+            "p50_s": s["p50_s"], "p99_s": s["p99_s"], "value": s["cell_updates_per_s"], "unit": UNIT,
+            "makespan_s": s["makespan_s"], "chunks": s["chunks"], "backlog_max": s["backlog_max"],
+            "peak_bytes": s["peak_bytes"],
+            "fp64_one_at_a_time": {"requests": baseline_req, "value": sb["cell_updates_per_s"],
+                                   "p50_s": sb["p50_s"], "p99_s": sb["p99_s"]}}
+
+
 def roofline(precision, cells, seconds_per_launch):
     peak, src = peaks()
     achieved = B_ALG[precision] * cells / seconds_per_launch / 1e9
@@ -239,6 +309,10 @@ def gpu_arm(args):
                          "ms_per_step": 1e3 * f32["seconds"] / args.steps,
                          "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
                          "clocks": f32["clocks"]}
+    if not args.no_batch:
+        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup)
+    if not args.no_serve:
+        forms["serving"] = bench_serving(nreq=args.serve_requests)
     cells = main["cells"]
     value = cells * args.steps * world / main["seconds"]
     line = {
@@ -299,6 +373,10 @@ def main():
     ap.add_argument("--band", type=int, default=8)
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--no-fp64", action="store_true", help="skip the fp64 form (profiling only)")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--serve-requests", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

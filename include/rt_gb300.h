@@ -121,6 +121,10 @@ int rt_get_state(rt_handle* h, double* E);
 /* Replaces integrate (integrate.f90:4-271, called at main.f90:70):
  * nsteps forward-Euler steps on the device-resident state. */
 int rt_integrate(rt_handle* h, int nsteps);
+/* Launch the step nsteps times from the current state WITHOUT advancing it
+ * (the spare buffer is overwritten).  For timing schedules (autotuner); the
+ * next rt_diagnose needs a real step first. */
+int rt_step_dry(rt_handle* h, int nsteps);
 /* One integrate on a host array, the literal drop-in for the module-state
  * call: E is uploaded, stepped once and written back (interior). */
 int rt_integrate_host(rt_handle* h, double* E);
@@ -175,6 +179,8 @@ int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph
 /* advance every member by nsteps (asynchronous on the batch stream) */
 int rt_batch_integrate(rt_batch* b, int nsteps);
 int rt_batch_sync(rt_batch* b);
+/* nsteps batch launches that do not advance the members (timing only) */
+int rt_batch_dry(rt_batch* b, int nsteps);
 int rt_batch_stream(rt_batch* b, void** stream);
 long long rt_batch_launch_count(const rt_batch* b);
 long long rt_batch_cells(const rt_batch* b);

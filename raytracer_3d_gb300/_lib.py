@@ -65,6 +65,8 @@ SIGNATURES = {
     "rt_version": (ctypes.c_char_p, []),
     "rt_set_schedule_sweep": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_sync": (ctypes.c_int, [_P]),
+    "rt_step_dry": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_batch_dry": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_cells": (ctypes.c_longlong, [_P]),
     "rt_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(_P)]),
     "rt_batch_destroy": (ctypes.c_int, [_P]),

@@ -437,6 +437,31 @@ int rt_batch_integrate(rt_batch* b, int nsteps) {
   return b->fp64 ? batch_run<double>(b, nsteps) : batch_run<float>(b, nsteps);
 }
 
+int rt_batch_dry(rt_batch* b, int nsteps) {
+  if (!b) return RT_ERR_ARG;
+  const int n = (int)b->mem.size();
+  for (int j = 0; j < n; j++) {
+    BCUDA_TRY(b, cudaEventRecord(b->mem[j]->ev, b->mem[j]->st));
+    BCUDA_TRY(b, cudaStreamWaitEvent(b->st, b->mem[j]->ev, 0));
+    if (b->mem[j]->cur != (b->cur0[j] ^ b->parity)) b->dirty = true;
+  }
+  if (b->dirty) {
+    int rc = b->fp64 ? batch_build<double>(b) : batch_build<float>(b);
+    if (rc) return rc;
+  }
+  for (int t = 0; t < nsteps; t++) {
+    cudaError_t e = b->fp64 ? batch_launch<double>(b, b->d_mem[b->parity]) : batch_launch<float>(b, b->d_mem[b->parity]);
+    if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
+    b->launches += 1;
+  }
+  BCUDA_TRY(b, cudaEventRecord(b->ev, b->st));
+  for (int j = 0; j < n; j++) {
+    BCUDA_TRY(b, cudaStreamWaitEvent(b->mem[j]->st, b->ev, 0));
+    b->mem[j]->steps_since_set = 0;
+  }
+  return RT_OK;
+}
+
 int rt_batch_sync(rt_batch* b) {
   if (!b) return RT_ERR_ARG;
   BCUDA_TRY(b, cudaStreamSynchronize(b->st));
@@ -787,6 +812,23 @@ int rt_integrate(rt_handle* h, int nsteps) {
     h->cur = 1 - h->cur;
     h->steps_since_set += 1;
   }
+  return RT_OK;
+}
+
+int rt_step_dry(rt_handle* h, int nsteps) {
+  if (!h) return RT_ERR_ARG;
+  if (nsteps < 0) return fail(h, RT_ERR_ARG, "rt_step_dry: nsteps < 0");
+  if (!h->have_coeff || !h->have_state) return fail(h, RT_ERR_STATE, "rt_step_dry: no state");
+  for (int t = 0; t < nsteps; t++) {
+    cudaError_t e;
+    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->tune, h->st);
+    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->tune, h->st);
+    h->launches += 1;
+    if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+  }
+  // the other buffer now holds E after one step; the state itself is unchanged,
+  // but a following rt_diagnose must not pair it with the old state
+  h->steps_since_set = 0;
   return RT_OK;
 }
 

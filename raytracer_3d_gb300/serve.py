@@ -1,0 +1,266 @@
+"""Serving loop: integrations requested over time, admitted against an HBM
+budget, kept device-resident and advanced together by continuous batching.
+
+A request is one wave-field integration (an `Experiment` plus a step
+count).  The loop:
+
+  1. admits arrived requests in arrival order while their device footprint
+     (resident fields plus the transient binary64 coefficient buffers of the
+     set-up) fits the budget; set-up of a new member runs on its own stream
+     while the current batch chunk runs on the batch stream;
+  2. advances every active member by one chunk of steps with one batched,
+     graph-captured launch per step (chunk = min(chunk_max, fewest steps any
+     member has left), so every member stops exactly at its step count);
+  3. retires finished members (state copied to the host, memory freed) and
+     repeats; new arrivals join at the next chunk boundary.
+
+Latency of a request = completion time - arrival time.  The executor is
+pluggable so the scheduling logic is testable without a GPU
+(`FakeExecutor`).
+"""
+import heapq
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Any, List, Optional
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    rid: int
+    exp: Any                 # configs.Experiment
+    steps: int
+    arrival: float           # seconds after the start of the run
+    cells: int = 0
+    admitted: Optional[float] = None
+    finished: Optional[float] = None
+    result: Any = None
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+
+def poisson_requests(n, rate, seed, steps_range=(50, 1000), spatial=None, spectral=None):
+    """n requests with exponential inter-arrival times (mean 1/rate s) and
+    step counts uniform in steps_range; dims as the ensemble members."""
+    from . import configs
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        kw = {}
+        if spatial:
+            kw["spatial"] = spatial
+        if spectral:
+            kw["spectral"] = spectral
+        exp = configs.ensemble_member(rng, steps=steps, **kw)
+        out.append(Request(i, exp, steps, t, cells=exp.cells))
+    return out
+
+
+def bytes_per_cell(precision):
+    """resident device bytes per cell and transient set-up bytes per cell"""
+    elem = 8 if precision == "fp64" else 4
+    nlam = 3 if precision == "fp64" else 1
+    resident = elem * (2 + 6 + nlam) + elem * 6 / 8.0      # + face-0 planes (<= n/8 of a field)
+    transient = 0 if precision == "fp64" else 8 * (6 + 3) + 8 * 6 / 8.0
+    return resident, transient
+
+
+@dataclass
+class ServeReport:
+    requests: List[Request]
+    makespan: float
+    cell_updates: int
+    peak_bytes: int
+    chunks: int
+    backlog_max: int
+    timeline: list = field(default_factory=list)
+
+    def percentile(self, q):
+        lat = sorted(r.latency for r in self.requests if r.latency is not None)
+        if not lat:
+            return None
+        k = max(0, min(len(lat) - 1, int(math.ceil(q / 100.0 * len(lat))) - 1))
+        return lat[k]
+
+    def summary(self):
+        return {"requests": len(self.requests),
+                "completed": sum(r.finished is not None for r in self.requests),
+                "p50_s": self.percentile(50), "p99_s": self.percentile(99),
+                "makespan_s": self.makespan,
+                "cell_updates_per_s": self.cell_updates / self.makespan if self.makespan > 0 else None,
+                "peak_bytes": self.peak_bytes, "chunks": self.chunks, "backlog_max": self.backlog_max}
+
+
+class Server:
+    def __init__(self, executor, budget_bytes=120e9, chunk_max=50, max_members=64):
+        self.ex = executor
+        self.budget = float(budget_bytes)
+        self.chunk_max = int(chunk_max)
+        self.max_members = int(max_members)
+
+    def run(self, requests):
+        ex = self.ex
+        queue = sorted(requests, key=lambda r: r.arrival)
+        qi = 0
+        active = []            # (request, member, remaining)
+        used = 0.0
+        peak = 0.0
+        chunks = 0
+        backlog_max = 0
+        total = 0
+        timeline = []
+        t0 = ex.now()
+        while qi < len(queue) or active:
+            now = ex.now() - t0
+            # ---- admission (arrival order, HBM budget) ----
+            while qi < len(queue) and queue[qi].arrival <= now and len(active) < self.max_members:
+                r = queue[qi]
+                need_res, need_tmp = ex.footprint(r)
+                if need_res + need_tmp > self.budget:
+                    raise ValueError("request %d needs %.3g B, more than the whole budget" % (r.rid, need_res + need_tmp))
+                if used + need_res + need_tmp > self.budget:
+                    break                                    # wait for memory to free up
+                member = ex.admit(r)                         # overlaps the running chunk
+                r.admitted = ex.now() - t0
+                used += need_res
+                peak = max(peak, used + need_tmp)
+                active.append([r, member, r.steps])
+                qi += 1
+            backlog = sum(1 for r in queue[qi:] if r.arrival <= now)
+            backlog_max = max(backlog_max, backlog)
+            if not active:
+                # idle until the next arrival
+                ex.wait_until(t0 + queue[qi].arrival)
+                continue
+            # ---- one chunk for all active members ----
+            n = min(self.chunk_max, min(a[2] for a in active))
+            ex.step([a[1] for a in active], n)
+            chunks += 1
+            total += n * sum(a[0].cells for a in active)
+            for a in active:
+                a[2] -= n
+            done = [a for a in active if a[2] == 0]
+            if done:
+                ex.sync()
+                for a in done:
+                    r = a[0]
+                    r.result = ex.retire(a[1])
+                    r.finished = ex.now() - t0
+                    used -= ex.footprint(r)[0]
+                active = [a for a in active if a[2] > 0]
+            timeline.append((ex.now() - t0, len(active), used))
+        makespan = ex.now() - t0
+        return ServeReport(queue, makespan, total, int(peak), chunks, backlog_max, timeline)
+
+
+class GpuExecutor:
+    """Members are `Model`s of libraytracer_gb300.so; a chunk is one
+    `Batch.integrate` (persistent, graph-captured launches)."""
+
+    def __init__(self, precision="fp32", tune=False, batch_tuning=None):
+        self.precision = precision
+        self.tune = tune
+        self.batch_tuning = batch_tuning
+        self._batch = None
+        self._members = None
+
+    def now(self):
+        return time.perf_counter()
+
+    def wait_until(self, t):
+        d = t - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+
+    def footprint(self, r):
+        res, tmp = bytes_per_cell(self.precision)
+        return res * r.cells, tmp * r.cells
+
+    def admit(self, r):
+        from .configs import build_model
+        return build_model(r.exp, self.precision)
+
+    def step(self, members, n):
+        from .batch import Batch
+        if self._members != [id(m) for m in members]:
+            if self._batch is not None:
+                self._batch.close()
+            self._batch = Batch(members)
+            if self.batch_tuning:
+                self._batch.set_tuning(*self.batch_tuning)
+            elif self.tune:
+                from .autotune import tune_batch
+                tune_batch(self._batch)
+            self._members = [id(m) for m in members]
+        self._batch.integrate(n)
+
+    def sync(self):
+        if self._batch is not None:
+            self._batch.sync()
+
+    def retire(self, member):
+        E = member.get_state().copy()
+        member.close()
+        return E
+
+    def close(self):
+        if self._batch is not None:
+            self._batch.close()
+            self._batch = None
+
+
+class SequentialExecutor(GpuExecutor):
+    """Baseline: one request at a time, each stepped alone (rt_integrate)."""
+
+    def step(self, members, n):
+        for m in members:
+            m.integrate(n)
+
+    def sync(self):
+        pass
+
+
+class FakeExecutor:
+    """Virtual-clock executor for CPU tests of the scheduling logic: a chunk
+    of n steps over members costs n * (launch + sum(cells) / rate) seconds,
+    admission costs setup_s; results record which steps each member saw."""
+
+    def __init__(self, rate=1e10, launch=1e-5, setup_s=1e-3, bpc=(36.0, 72.0)):
+        self.t = 0.0
+        self.rate = rate
+        self.launch = launch
+        self.setup_s = setup_s
+        self.bpc = bpc
+        self.log = []
+
+    def now(self):
+        return self.t
+
+    def wait_until(self, t):
+        self.t = max(self.t, t)
+
+    def footprint(self, r):
+        return self.bpc[0] * r.cells, self.bpc[1] * r.cells
+
+    def admit(self, r):
+        self.t += self.setup_s
+        return {"rid": r.rid, "steps": 0, "cells": r.cells}
+
+    def step(self, members, n):
+        self.t += n * (self.launch + sum(m["cells"] for m in members) / self.rate)
+        for m in members:
+            m["steps"] += n
+        self.log.append((self.t, [m["rid"] for m in members], n))
+
+    def sync(self):
+        pass
+
+    def retire(self, member):
+        return member["steps"]

@@ -224,3 +224,14 @@ def test_single_precision_literals():
     assert float(np.float32(1e20)) == 1.0000000200408773e20
     assert float(np.float32(np.pi)) == 3.1415927410125732
     assert float(np.float32(1e-12)) == 9.999999960041972e-13
+
+
+def test_ensemble_grids_pass_reference_checks():
+    # every dims combination of the batched / served workloads builds a grid
+    # that the reference's calc_grid accepts
+    import itertools
+    from raytracer_3d_gb300.configs import SPATIAL_DIMS, SPECTRAL_DIMS, ensemble_member
+    rng = np.random.default_rng(0)
+    for nz, nm in itertools.product(SPATIAL_DIMS + (4, 6), SPECTRAL_DIMS + (4, 6)):
+        e = ensemble_member(rng, spatial=(nz,), spectral=(nm,))
+        calc_grid(e.n, e.d_interior, e.fixed)
