@@ -159,6 +159,27 @@ long long rt_device_bytes(const rt_handle* h);
 /* library version string */
 const char* rt_version(void);
 
+/* ---- allocation-free entry point --------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host framework that owns every device allocation, allocations frozen
+ * during graph capture or a real-time loop, no out-of-memory failure
+ * allowed mid-run): the CFL rate of rt_max_rate computed from device arrays
+ * the caller owns, allocating nothing.
+ *   vel[a]   right-face velocities of axis a, cell-shaped, unpadded, x fastest
+ *   vlo[a]   face-0 velocities of axis a (cell shape with axis a collapsed)
+ *   dgrid[a] padded grid spacing of axis a (n_a + 4 doubles)
+ *   out      one device double; receives the rate
+ * Inactive axes (n = 1) may pass NULL.  Runs asynchronously on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  Its scratch is a fixed
+ * 256 KiB device array inside the library, so fields above 2^31 cells are
+ * rejected with RT_ERR_ARG.  The first call on a device looks up that
+ * array's address and must come before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race.  Errors are described by
+ * rt_noalloc_last_error(). */
+int rt_max_rate_noalloc(const rt_dims* dims, const double* const* vel, const double* const* vlo,
+                        const double* const* dgrid, double* out, void* stream);
+const char* rt_noalloc_last_error(void);
+
 /* ---- batched ensemble -------------------------------------------------
  * No counterpart in the reference, which advances one field per run: a
  * batch advances many independent fields (members) of possibly different

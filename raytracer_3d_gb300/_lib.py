@@ -77,6 +77,9 @@ SIGNATURES = {
     "rt_batch_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "rt_batch_launch_count": (ctypes.c_longlong, [_P]),
     "rt_batch_cells": (ctypes.c_longlong, [_P]),
+    "rt_max_rate_noalloc": (ctypes.c_int, [ctypes.POINTER(RtDims), ctypes.POINTER(_D), ctypes.POINTER(_D),
+                                           ctypes.POINTER(_D), _D, _P]),
+    "rt_noalloc_last_error": (ctypes.c_char_p, []),
 }
 
 _lib = None
