@@ -176,13 +176,22 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None):
+FP32_CANDIDATES = [(v, b, t, s) for v in ("tma", "group") for t in (256, 512, 1024) for b in (4, 8)
+                   for s in (0, 1)]
+
+
+def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False):
     import numpy as np
     import torch
     from raytracer_3d_gb300 import configs
     exp = configs.jet_large(n=n)
     m = configs.build_model(exp, precision)
-    if sched:
+    tuned = None
+    table = None
+    if tune:
+        from raytracer_3d_gb300.autotune import tune_model
+        tuned, table = tune_model(m, candidates=FP32_CANDIDATES, reps=2, use_cache=False)
+    elif sched:
         m.set_tuning(*sched)
     cells = exp.cells
     m.integrate(warmup)
@@ -191,7 +200,10 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None):
     with ClockSampler(torch.cuda.current_device()) as cs:
         secs, launches = time_steps(m, steps)
     secs = max_over_ranks(dist, secs)
-    out = {"cells": cells, "seconds": secs, "launches": launches, "clocks": cs.summary(), "dt": m.dt}
+    out = {"cells": cells, "seconds": secs, "launches": launches, "clocks": cs.summary(), "dt": m.dt,
+           "schedule": tuned or sched,
+           "tuning_table_ms": None if table is None else [["%s b%d t%d s%d" % c, round(1e3 * t, 3)]
+                                                           for c, t in table]}
     # end to end through the host-array drop-in (rt_integrate_host)
     if e2e_steps > 0:
         m.get_state()
@@ -262,7 +274,7 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
     fp64 one-at-a-time baseline on the first requests."""
     from raytracer_3d_gb300.serve import GpuExecutor, SequentialExecutor, Server, poisson_requests
     reqs = poisson_requests(nreq, rate=rate, seed=seed)
-    ex = GpuExecutor("fp32", batch_tuning=(8, 256, 0, 16))
+    ex = GpuExecutor("fp32", batch_tuning=(8, 1024, 0, 16))
     rep = Server(ex, budget_bytes=budget, chunk_max=50).run(reqs)
     ex.close()
     s = rep.summary()
@@ -294,19 +306,23 @@ def roofline(precision, cells, seconds_per_launch):
 def gpu_arm(args):
     rank, world, local, dist = dist_init(args.gpus)
     n = (args.n,) * 6
-    sched = (args.variant, args.band, args.threads)
+    sched = (args.variant, args.band, args.threads, args.sweep)
     if args.no_fp64:  # profiling runs of the fp32 form only
-        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched)
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
         if rank == 0:
             print(json.dumps({"profile_only": "fp32", "cells": f32["cells"],
                               "ms_per_step": 1e3 * f32["seconds"] / args.steps}), flush=True)
         return
-    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, sched)
+    # the binary64 form is bound by the FP64 pipe; 256-thread CTAs keep its
+    # registers unspilled (the flags set the fp32 schedule when --tune 0)
+    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, ("tma", 8, 256, 0))
     forms = {}
     if not args.no_fp32:
-        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched)
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
         forms["fp32"] = {"value": f32["cells"] * args.steps * world / f32["seconds"],
                          "ms_per_step": 1e3 * f32["seconds"] / args.steps,
+                         "schedule": "%s band %d threads %d sweep %d" % tuple(f32["schedule"]),
+                         "tuning_table_ms": f32["tuning_table_ms"],
                          "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
                          "clocks": f32["clocks"]}
     if not args.no_batch:
@@ -321,7 +337,7 @@ def gpu_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded log-normal spectrum, analytic N(z), U(y,z))",
         "config": {"workload": "jet_large %d^3x%d^3 plain fp64, CFL 0.4 (dt=%%.6g s)" % (n[0], n[0]) % main["dt"],
-                   "cells": cells, "form": "fp64", "schedule": "%s band %d threads %d" % sched, "l2": "state 8.6 GB per field >> L2; no flush needed",
+                   "cells": cells, "form": "fp64", "schedule": "tma band 8 threads 256 sweep 0", "l2": "state 8.6 GB per field >> L2; no flush needed",
                    "parallelism": "replicas x%d" % world},
         "roofline": roofline("fp64", cells, main["seconds"] / args.steps),
         "clocks": main["clocks"],
@@ -369,9 +385,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
-    ap.add_argument("--variant", default="tma", choices=("tma", "plane", "cell"))
+    ap.add_argument("--variant", default="tma", choices=("tma", "group", "plane", "cell"))
     ap.add_argument("--band", type=int, default=8)
-    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--threads", type=int, default=1024)
+    ap.add_argument("--sweep", type=int, default=0)
+    ap.add_argument("--tune", type=int, default=1, help="autotune the fp32 schedule (1) or use the flags (0)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the fp64 form (profiling only)")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")

@@ -138,9 +138,10 @@ int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int,
 
 /* Schedule of the step kernel (no effect on results).  variant: 2 = plane
  * tiled with bulk-copy (TMA) staging of the E planes (default; used when a
- * plane of E is a multiple of 16 bytes), 0 = plane tiled with plain loads,
+ * plane of E is a multiple of 16 bytes), 3 = the same with several z planes
+ * per work item (for small x-y planes), 0 = plane tiled with plain loads,
  * 1 = one thread per cell; band: values per band of the plane schedule
- * (default 8); threads: CTA size 128, 256 or 512.  Chosen by the autotuner
+ * (default 8); threads: CTA size 128, 256, 512 or 1024 (default 512).  Chosen by the autotuner
  * (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);
 /* Sweep order of the plane schedule: 0 = bands over m (default), 1 = bands
@@ -194,7 +195,7 @@ typedef struct rt_batch rt_batch;
 int rt_batch_create(rt_handle* const* members, int n, rt_batch** out);
 int rt_batch_destroy(rt_batch* b);
 const char* rt_batch_last_error(const rt_batch* b);
-/* band, CTA size (128/256/512), sweep order (0/1) and steps per captured
+/* band, CTA size (128/256/512/1024), sweep order (0/1) and steps per captured
  * graph (even); chosen by the autotuner (raytracer_3d_gb300.autotune) */
 int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps);
 /* advance every member by nsteps (asynchronous on the batch stream) */

@@ -14,10 +14,11 @@ import time
 
 DEFAULT_CANDIDATES = [
     (variant, band, threads, sweep)
-    for variant in ("tma", "plane")
-    for threads in (256, 512)
+    for variant in ("tma", "group", "plane")
+    for threads in (256, 512, 1024)
     for band in (4, 8, 16)
     for sweep in (0, 1)
+    if not (variant == "plane" and threads == 1024)
 ]
 
 
@@ -94,7 +95,7 @@ def tune_model(model, candidates=None, reps=3, use_cache=True):
 
 BATCH_CANDIDATES = [
     (band, threads, sweep)
-    for threads in (256, 512)
+    for threads in (256, 512, 1024)
     for band in (4, 8, 16)
     for sweep in (0, 1)
 ]

@@ -42,6 +42,8 @@ struct rt_handle {
   void* vel[6]{};
   void* vlo[6]{};
   void* lam[3]{};
+  double* uc[6]{};              // binary64 form: cached uCFL of the right faces
+  double* ucl[6]{};             // and of the face-0 planes
   void* E[2]{};
   int cur = 0;
   double* scratch = nullptr;    // reductions
@@ -91,9 +93,11 @@ static int dev_alloc(rt_handle* h, void** ptr, size_t n) {
   return RT_OK;
 }
 
-// transient device buffer (not counted in the handle's resident bytes)
+// transient device buffer (not counted in the handle's resident bytes),
+// stream-ordered on the handle's stream so that allocating and freeing it
+// does not synchronise with work running on other streams (a batch)
 static int tmp_alloc(rt_handle* h, void** ptr, size_t n) {
-  cudaError_t e = cudaMalloc(ptr, n);
+  cudaError_t e = cudaMallocAsync(ptr, n, h->st);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *ptr = nullptr;
@@ -185,11 +189,27 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
     A.vlo[a] = (const T*)h->vlo[a];
   }
   for (int c = 0; c < 3; c++) A.lam[c] = (const T*)h->lam[c];
+  for (int a = 0; a < 6; a++) {
+    A.uc[a] = (const T*)h->uc[a];
+    A.ucl[a] = (const T*)h->ucl[a];
+  }
   A.E = (const T*)h->E[src];
   A.Enew = (T*)h->E[1 - src];
   A.dt = h->p.dt;
   A.status = h->status;
   return A;
+}
+
+// binary64 form: refresh the cached uCFL fields (after the coefficients or dt change)
+static int refresh_ucfl(rt_handle* h) {
+  if (h->p.precision != RT_FP64 || !h->have_coeff) return RT_OK;
+  const double* vel[6];
+  const double* vlo[6];
+  for (int a = 0; a < 6; a++) { vel[a] = (const double*)h->vel[a]; vlo[a] = (const double*)h->vlo[a]; }
+  cudaError_t e = launch_ucfl(h->d, make_grid(h), h->p.dt, vel, vlo, h->uc, h->ucl, h->st);
+  h->launches += 6;
+  if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "uCFL: %s", cudaGetErrorString(e));
+  return RT_OK;
 }
 
 // binary32 tables 1/d and dt/d on the padded range
@@ -228,6 +248,8 @@ struct rt_batch {
   long long* d_first = nullptr;
   size_t smem = 0;
   bool tma = false;
+  bool group = false;           // z-group items (rt_step4.cuh)
+  long long max_nxy = 0;
   StepTuning tune;
   int grid = 0;
   int graph_steps = 16;         // steps per captured graph (even)
@@ -265,7 +287,9 @@ static void batch_free_graphs(rt_batch* b) {
 template <class T>
 static cudaError_t batch_launch(rt_batch* b, const void* mem) {
   const int n = (int)b->mem.size();
-  if (b->tma) return launch_batch_tma<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
+  if (b->group) return launch_batch_group<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
+  if (b->tma)
+    return launch_batch_tma<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->max_nxy, b->st);
   return launch_batch<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
 }
 
@@ -275,19 +299,33 @@ static int batch_build(rt_batch* b) {
   std::vector<BatchMember<T>> arr[2];
   std::vector<long long> first(n + 1, 0);
   size_t smem = 0;
-  bool tma = true;
-  for (int j = 0; j < n; j++) tma = tma && tma_path_ok<T>(b->mem[j]->d);
+  bool tma = true, group = true;
+  b->max_nxy = 0;
+  std::vector<int> gz(n, 1);
+  for (int j = 0; j < n; j++) {
+    tma = tma && tma_path_ok<T>(b->mem[j]->d);
+    gz[j] = group_size<T>(b->mem[j]->d, b->tune);
+    group = group && gz[j] > 0;
+    b->max_nxy = std::max(b->max_nxy, (long long)b->mem[j]->d.n[0] * b->mem[j]->d.n[1]);
+  }
+  // z-group items are preferred: they keep the CTA busy on small planes
+  if (group) tma = false;
+  // the TMA plane kernel covers the largest plane with at most RT_TMA_MAXC cells per thread
+  if ((b->max_nxy + b->tune.threads - 1) / b->tune.threads > RT_TMA_MAXC) tma = false;
+  // the plain-load batch kernel has no 1024-thread form
+  if (!tma && !group && b->tune.threads > 512) b->tune.threads = 512;
   for (int j = 0; j < n; j++) {
     rt_handle* h = b->mem[j];
     StepTuning tn = b->tune;
     for (int par = 0; par < 2; par++) {
       BatchMember<T> bm;
       bm.A = make_step_args<T>(h, par == 0 ? h->cur : 1 - h->cur);
-      bm.S = make_sched(h->d, tn);
+      bm.S = make_sched(h->d, tn, group ? gz[j] : 1);
       arr[par].push_back(bm);
     }
     first[j + 1] = first[j] + sched_items(h->d, arr[0].back().S);
-    smem = std::max(smem, tma ? tma_path_smem<T>(h->d) : plane_smem<T>(h->d));
+    smem = std::max(smem, group ? group_path_smem<T>(h->d, gz[j])
+                                : (tma ? tma_path_smem<T>(h->d) : plane_smem<T>(h->d)));
     b->cur0[j] = h->cur;
   }
   for (int par = 0; par < 2; par++) {
@@ -300,10 +338,11 @@ static int batch_build(rt_batch* b) {
                           cudaMemcpyHostToDevice));
   b->smem = smem;
   b->tma = tma;
+  b->group = group;
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int per_sm = batch_blocks_per_sm<T>(b->tune.threads, smem, tma);
+  const int per_sm = batch_blocks_per_sm<T>(b->tune.threads, smem, tma, group);
   if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batch kernel does not fit on an SM");
   const long long items = first[n];
   b->grid = (int)std::min<long long>(items, (long long)per_sm * nsm);
@@ -418,8 +457,8 @@ const char* rt_batch_last_error(const rt_batch* b) { return b ? b->err.c_str() :
 int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps) {
   if (!b) return RT_ERR_ARG;
   if (band < 1 || band > 1024) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: band %d out of range", band);
-  if (threads != 128 && threads != 256 && threads != 512)
-    return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: threads must be 128, 256 or 512");
+  if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)
+    return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: threads must be 128, 256, 512 or 1024");
   if (sweep != 0 && sweep != 1) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: sweep must be 0 or 1");
   if (graph_steps < 2 || graph_steps % 2) return bfail(b, RT_ERR_ARG, "rt_batch_set_tuning: graph_steps must be even and >= 2");
   cudaStreamSynchronize(b->st);
@@ -526,6 +565,7 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
   d.nspec = (long long)nn[3] * nn[4] * nn[5];
   d.upper_refl = params->enable_upper_reflection ? 1 : 0;
   d.lower_refl = params->enable_lower_reflection ? 1 : 0;
+  fill_plane_strides(d);
   h->elem = params->precision == RT_FP64 ? 8 : 4;
 
   auto bail = [&](int code) {
@@ -557,6 +597,11 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
   const int nlam = params->precision == RT_FP64 ? 3 : 1;
   for (int c = 0; c < nlam; c++)
     if ((rc = dev_alloc(h, &h->lam[c], fb))) return bail(rc);
+  if (params->precision == RT_FP64)
+    for (int a = 0; a < 6; a++) {
+      if ((rc = dev_alloc(h, (void**)&h->uc[a], fb))) return bail(rc);
+      if ((rc = dev_alloc(h, (void**)&h->ucl[a], (size_t)(d.ncell / d.n[a]) * 8))) return bail(rc);
+    }
   const DiagSizes ds = diag_sizes(d);
   h->scratch_len = std::max(ds.scratch_doubles(), max_rate_partials(d)) + 8;
   if ((rc = dev_alloc(h, (void**)&h->scratch, h->scratch_len * sizeof(double)))) return bail(rc);
@@ -577,6 +622,7 @@ int rt_destroy(rt_handle* h) {
   for (int k = 0; k < 2; k++) cudaFree(h->E[k]);
   for (int a = 0; a < 6; a++) { cudaFree(h->vel[a]); cudaFree(h->vlo[a]); }
   for (int c = 0; c < 3; c++) cudaFree(h->lam[c]);
+  for (int a = 0; a < 6; a++) { cudaFree(h->uc[a]); cudaFree(h->ucl[a]); }
   cudaFree(h->scratch);
   cudaFree(h->vol3);
   cudaFree(h->result);
@@ -626,8 +672,11 @@ int rt_set_dt(rt_handle* h, double dt) {
   if (!h) return RT_ERR_ARG;
   if (!(dt > 0.0)) return fail(h, RT_ERR_ARG, "rt_set_dt: dt must be > 0");
   h->p.dt = dt;
-  if (h->have_grid) return upload_tab32(h);
-  return RT_OK;
+  if (h->have_grid) {
+    int rc = upload_tab32(h);
+    if (rc) return rc;
+  }
+  return refresh_ucfl(h);
 }
 
 int rt_calc_parameter(rt_handle* h) {
@@ -698,11 +747,12 @@ int rt_calc_parameter(rt_handle* h) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) { rc = fail(h, RT_ERR_CUDA, "calc_parameter: %s", cudaGetErrorString(e)); goto cleanup; }
   }
-  rc = RT_OK;
   h->have_coeff = true;
+  rc = refresh_ucfl(h);
 cleanup:
-  cudaStreamSynchronize(h->st);  // no kernel may still read a temporary
-  for (void* p : tmp) { cudaFree(p); }
+  // stream-ordered frees run after the kernels that read the temporaries
+  for (void* p : tmp) { cudaFreeAsync(p, h->st); }
+  cudaStreamSynchronize(h->st);
   return rc;
 }
 
@@ -899,11 +949,12 @@ int rt_diagnose(rt_handle* h, rt_budget* o, double* E_int, double* meanfl_int, d
 
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
   if (!h) return RT_ERR_ARG;
-  if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA)
+  if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA &&
+      variant != RT_VARIANT_GROUP)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
-  if (threads != 128 && threads != 256 && threads != 512)
-    return fail(h, RT_ERR_ARG, "rt_set_tuning: threads must be 128, 256 or 512");
+  if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)
+    return fail(h, RT_ERR_ARG, "rt_set_tuning: threads must be 128, 256, 512 or 1024");
   h->tune.variant = variant;
   h->tune.band = band;
   h->tune.threads = threads;

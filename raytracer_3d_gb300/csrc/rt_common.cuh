@@ -23,6 +23,7 @@ namespace rt {
 struct Dims {
   int n[6];            // nx ny nz nk nl nm
   long long s[6];      // strides of the unpadded 6D arrays (s[0] = 1)
+  long long ps[6][6];  // ps[a][b]: stride along b of the face-0 plane of axis a
   long long ncell;     // product of n
   long long nvol3;     // nx*ny*nz
   long long nspec;     // nk*nl*nm
@@ -49,8 +50,16 @@ struct Background {
 __host__ __device__ __forceinline__ int pidx(int f) { return f + RT_ONX - 1; }
 
 // stride of the plane vel_lo[a] along axis b (axis a collapsed)
-__host__ __device__ __forceinline__ long long plane_stride(const Dims& d, int a, int b) {
+__host__ __device__ __forceinline__ long long plane_stride_calc(const Dims& d, int a, int b) {
   return b < a ? d.s[b] : (b == a ? 0 : d.s[b] / d.n[a]);
+}
+__host__ __device__ __forceinline__ long long plane_stride(const Dims& d, int a, int b) {
+  return d.ps[a][b];
+}
+// fill d.ps from d.n and d.s (host side, once per handle)
+__host__ __forceinline__ void fill_plane_strides(Dims& d) {
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) d.ps[a][b] = plane_stride_calc(d, a, b);
 }
 
 // ---- exact binary64 arithmetic (never contracted into FMA) --------------

@@ -8,6 +8,7 @@
 #include "rt_step.cuh"
 #include "rt_step2.cuh"
 #include "rt_step3.cuh"
+#include "rt_step4.cuh"
 
 namespace rt {
 
@@ -133,6 +134,31 @@ __global__ void lam_combine_kernel(const double* lx, const double* ly, const dou
     if (uz) s += lz[i];
     dst[i] = __double2float_rn(s);
   }
+}
+
+// uCFL = |v*dt/d(f)| of every face of axis a (binary64 form), in the order of
+// superbee_fluxes.f90:19: right faces f = c_a + 1 and the face-0 plane
+__global__ void ucfl_kernel(Dims d, Grid g, int a, double dt, const double* vel, const double* vlo,
+                            double* uc, double* ucl) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < d.ncell; p += stride) {
+    const int ca = (int)((p / d.s[a]) % d.n[a]);
+    uc[p] = fabs(ddiv(dmul(vel[p], dt), g.d[a][pidx(ca + 1)]));
+  }
+  const long long np = d.ncell / d.n[a];
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < np; q += stride)
+    ucl[q] = fabs(ddiv(dmul(vlo[q], dt), g.d[a][pidx(0)]));
+}
+
+cudaError_t launch_ucfl(const Dims& d, const Grid& g, double dt, const double* const* vel,
+                        const double* const* vlo, double* const* uc, double* const* ucl,
+                        cudaStream_t st) {
+  for (int a = 0; a < 6; a++) {
+    ucfl_kernel<<<8 * 152, 256, 0, st>>>(d, g, a, dt, vel[a], vlo[a], uc[a], ucl[a]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------
@@ -493,16 +519,39 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
   return cudaGetLastError();
 }
 
-PlaneSched make_sched(const Dims& d, const StepTuning& tn) {
+PlaneSched make_sched(const Dims& d, const StepTuning& tn, int gz) {
   PlaneSched S;
   S.sweep = tn.sweep ? 1 : 0;
   const int nb = S.sweep ? d.n[4] : d.n[5];
   S.band = tn.band > 0 ? tn.band : 8;
   if (S.band > nb) S.band = nb;
   S.nband = (nb + S.band - 1) / S.band;
-  S.nunits = (long long)d.n[2] * d.n[3];
+  S.gz = gz > 0 ? gz : 1;
+  S.nunits = (long long)((d.n[2] + S.gz - 1) / S.gz) * d.n[3];
   return S;
 }
+PlaneSched make_sched(const Dims& d, const StepTuning& tn) { return make_sched(d, tn, 1); }
+
+template <class T>
+size_t group_path_smem(const Dims& d, int G) { return group_smem<T>(d, G); }
+template size_t group_path_smem<double>(const Dims&, int);
+template size_t group_path_smem<float>(const Dims&, int);
+
+// z planes per item: about one cell per thread, at most nz, at most 4096
+// cells per item (the coordinate multiply), shared memory within 200 KB
+template <class T>
+int group_size(const Dims& d, const StepTuning& tn) {
+  const long long nxy = (long long)d.n[0] * d.n[1];
+  if (!tma_ok<T>(d) || nxy > 4096) return 0;
+  int G = tn.group > 0 ? tn.group : (int)(tn.threads / nxy);
+  if (G < 1) G = 1;
+  if (G > d.n[2]) G = d.n[2];
+  while (G > 1 && ((long long)(G + 1) * nxy > 4096 || group_smem<T>(d, G) > 200 * 1024)) G--;
+  if ((long long)(G + 1) * nxy > 4096 * 2 || group_smem<T>(d, G) > 200 * 1024) return 0;
+  return G;
+}
+template int group_size<double>(const Dims&, const StepTuning&);
+template int group_size<float>(const Dims&, const StepTuning&);
 
 long long sched_items(const Dims& d, const PlaneSched& S) {
   const int nouter = S.sweep ? d.n[5] : d.n[4];
@@ -519,8 +568,17 @@ template size_t plane_smem<float>(const Dims&);
 template bool plane_ok<double>(const Dims&);
 template bool plane_ok<float>(const Dims&);
 
+// the TMA path: planes a multiple of 16 bytes, shared memory within 200 KB,
+// at most 4096 cells per plane (the coordinate multiply of tma_item), and at
+// most RT_TMA_MAXC cells per thread for the largest CTA (checked again for
+// the CTA size actually launched)
 template <class T>
-bool tma_path_ok(const Dims& d) { return tma_ok<T>(d) && tma_smem<T>(d) <= 200 * 1024; }
+bool tma_path_ok(const Dims& d) {
+  const long long nxy = (long long)d.n[0] * d.n[1];
+  return tma_ok<T>(d) && tma_smem<T>(d) <= 200 * 1024 && nxy <= 4096 && nxy <= RT_TMA_MAXC * 1024LL;
+}
+// cells per thread of the TMA kernels for a CTA of nt threads
+static int tma_maxc(long long nxy, int nt) { return (int)((nxy + nt - 1) / nt); }
 template <class T>
 size_t tma_path_smem(const Dims& d) { return tma_smem<T>(d); }
 template bool tma_path_ok<double>(const Dims&);
@@ -533,23 +591,55 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+template <class T, int NT, int MAXC>
+static cudaError_t launch_tma_nt_c(const StepArgs<T>& A, const PlaneSched& S, long long nblk,
+                                   cudaStream_t st) {
+  const size_t sm = tma_smem<T>(A.d);
+  cudaError_t e = set_smem<T, NT>(step_tma_kernel<T, NT, MAXC>, sm);
+  if (e != cudaSuccess) return e;
+  step_tma_kernel<T, NT, MAXC><<<(unsigned)nblk, NT, sm, st>>>(A, S);
+  return cudaGetLastError();
+}
+
 template <class T, int NT>
 static cudaError_t launch_tma_nt(const StepArgs<T>& A, const PlaneSched& S, long long nblk,
                                  cudaStream_t st) {
-  const size_t sm = tma_smem<T>(A.d);
-  cudaError_t e = set_smem<T, NT>(step_tma_kernel<T, NT>, sm);
+  const int mc = tma_maxc((long long)A.d.n[0] * A.d.n[1], NT);
+  if (mc <= 1) return launch_tma_nt_c<T, NT, 1>(A, S, nblk, st);
+  if (mc <= 2) return launch_tma_nt_c<T, NT, 2>(A, S, nblk, st);
+  return launch_tma_nt_c<T, NT, 4>(A, S, nblk, st);
+}
+
+template <class T, int NT>
+static cudaError_t launch_group_nt(const StepArgs<T>& A, const PlaneSched& S, long long nblk,
+                                   cudaStream_t st) {
+  const size_t sm = group_smem<T>(A.d, S.gz);
+  cudaError_t e = set_smem<T, NT>(step_group_kernel<T, NT>, sm);
   if (e != cudaSuccess) return e;
-  step_tma_kernel<T, NT><<<(unsigned)nblk, NT, sm, st>>>(A, S);
+  step_group_kernel<T, NT><<<(unsigned)nblk, NT, sm, st>>>(A, S);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st) {
-  if (tn.variant == RT_VARIANT_TMA && tma_path_ok<T>(A.d)) {
+  if (tn.variant == RT_VARIANT_GROUP) {
+    const int G = group_size<T>(A.d, tn);
+    if (G > 0) {
+      const PlaneSched S = make_sched(A.d, tn, G);
+      const long long nblk = sched_items(A.d, S);
+      if (tn.threads == 128) return launch_group_nt<T, 128>(A, S, nblk, st);
+      if (tn.threads == 512) return launch_group_nt<T, 512>(A, S, nblk, st);
+      if (tn.threads == 1024) return launch_group_nt<T, 1024>(A, S, nblk, st);
+      return launch_group_nt<T, 256>(A, S, nblk, st);
+    }
+  }
+  if (tn.variant == RT_VARIANT_TMA && tma_path_ok<T>(A.d) &&
+      tma_maxc((long long)A.d.n[0] * A.d.n[1], tn.threads) <= RT_TMA_MAXC) {
     const PlaneSched S = make_sched(A.d, tn);
     const long long nblk = sched_items(A.d, S);
     if (tn.threads == 128) return launch_tma_nt<T, 128>(A, S, nblk, st);
     if (tn.threads == 512) return launch_tma_nt<T, 512>(A, S, nblk, st);
+    if (tn.threads == 1024) return launch_tma_nt<T, 1024>(A, S, nblk, st);
     return launch_tma_nt<T, 256>(A, S, nblk, st);
   }
   if ((tn.variant == RT_VARIANT_PLANE || tn.variant == RT_VARIANT_TMA) && plane_ok<T>(A.d)) {
@@ -558,7 +648,7 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
     const size_t sm = plane_smem<T>(A.d);
     if (tn.threads == 128)
       step_plane_kernel<T, 128><<<(unsigned)nblk, 128, sm, st>>>(A, S);
-    else if (tn.threads == 512)
+    else if (tn.threads >= 512)
       step_plane_kernel<T, 512><<<(unsigned)nblk, 512, sm, st>>>(A, S);
     else
       step_plane_kernel<T, 256><<<(unsigned)nblk, 256, sm, st>>>(A, S);
@@ -576,7 +666,7 @@ cudaError_t launch_batch(const void* members, const long long* first, int nmem, 
   const BatchMember<T>* mem = (const BatchMember<T>*)members;
   if (threads == 128)
     batch_plane_kernel<T, 128><<<grid, 128, smem, st>>>(mem, first, nmem);
-  else if (threads == 512)
+  else if (threads >= 512)
     batch_plane_kernel<T, 512><<<grid, 512, smem, st>>>(mem, first, nmem);
   else
     batch_plane_kernel<T, 256><<<grid, 256, smem, st>>>(mem, first, nmem);
@@ -586,13 +676,20 @@ template cudaError_t launch_batch<double>(const void*, const long long*, int, si
 template cudaError_t launch_batch<float>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
 
 template <class T, int NT>
-static int occ_batch(bool tma, size_t smem) {
+static int occ_batch(bool tma, size_t smem, bool group = false) {
   int nb = 0;
   cudaError_t e;
-  if (tma) {
-    e = set_smem<T, NT>(batch_tma_kernel<T, NT>, smem);
+  if (group) {
+    e = set_smem<T, NT>(batch_group_kernel<T, NT>, smem);
     if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_tma_kernel<T, NT>, NT, smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_group_kernel<T, NT>, NT, smem);
+  } else if (tma) {
+    // one MAXC for the occupancy query: register use differs little
+    e = set_smem<T, NT>(batch_tma_kernel<T, NT, 1>, smem);
+    if (e == cudaSuccess) e = set_smem<T, NT>(batch_tma_kernel<T, NT, 2>, smem);
+    if (e == cudaSuccess) e = set_smem<T, NT>(batch_tma_kernel<T, NT, 4>, smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_tma_kernel<T, NT, 4>, NT, smem);
   } else {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_plane_kernel<T, NT>, NT, smem);
   }
@@ -601,28 +698,50 @@ static int occ_batch(bool tma, size_t smem) {
 }
 
 template <class T>
-int batch_blocks_per_sm(int threads, size_t smem, bool tma) {
-  if (threads == 128) return occ_batch<T, 128>(tma, smem);
-  if (threads == 512) return occ_batch<T, 512>(tma, smem);
-  return occ_batch<T, 256>(tma, smem);
+int batch_blocks_per_sm(int threads, size_t smem, bool tma, bool group) {
+  if (threads == 128) return occ_batch<T, 128>(tma, smem, group);
+  if (threads == 512) return occ_batch<T, 512>(tma, smem, group);
+  if (threads == 1024) return (tma || group) ? occ_batch<T, 1024>(tma, smem, group) : 0;
+  return occ_batch<T, 256>(tma, smem, group);
 }
-template int batch_blocks_per_sm<double>(int, size_t, bool);
-template int batch_blocks_per_sm<float>(int, size_t, bool);
+template int batch_blocks_per_sm<double>(int, size_t, bool, bool);
+template int batch_blocks_per_sm<float>(int, size_t, bool, bool);
+
+template <class T>
+cudaError_t launch_batch_group(const void* members, const long long* first, int nmem, size_t smem,
+                               int threads, int grid, cudaStream_t st) {
+  const BatchMember<T>* mem = (const BatchMember<T>*)members;
+  if (threads == 128) batch_group_kernel<T, 128><<<grid, 128, smem, st>>>(mem, first, nmem);
+  else if (threads == 512) batch_group_kernel<T, 512><<<grid, 512, smem, st>>>(mem, first, nmem);
+  else if (threads == 1024) batch_group_kernel<T, 1024><<<grid, 1024, smem, st>>>(mem, first, nmem);
+  else batch_group_kernel<T, 256><<<grid, 256, smem, st>>>(mem, first, nmem);
+  return cudaGetLastError();
+}
+template cudaError_t launch_batch_group<double>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+template cudaError_t launch_batch_group<float>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+
+template <class T, int NT>
+static void batch_tma_nt(const BatchMember<T>* mem, const long long* first, int nmem, size_t smem,
+                         int maxc, int grid, cudaStream_t st) {
+  if (maxc <= 1) batch_tma_kernel<T, NT, 1><<<grid, NT, smem, st>>>(mem, first, nmem);
+  else if (maxc <= 2) batch_tma_kernel<T, NT, 2><<<grid, NT, smem, st>>>(mem, first, nmem);
+  else batch_tma_kernel<T, NT, 4><<<grid, NT, smem, st>>>(mem, first, nmem);
+}
 
 template <class T>
 cudaError_t launch_batch_tma(const void* members, const long long* first, int nmem, size_t smem,
-                             int threads, int grid, cudaStream_t st) {
+                             int threads, int grid, long long max_nxy, cudaStream_t st) {
   const BatchMember<T>* mem = (const BatchMember<T>*)members;
-  if (threads == 128)
-    batch_tma_kernel<T, 128><<<grid, 128, smem, st>>>(mem, first, nmem);
-  else if (threads == 512)
-    batch_tma_kernel<T, 512><<<grid, 512, smem, st>>>(mem, first, nmem);
-  else
-    batch_tma_kernel<T, 256><<<grid, 256, smem, st>>>(mem, first, nmem);
+  const int mc = tma_maxc(max_nxy, threads);
+  if (mc > RT_TMA_MAXC) return cudaErrorInvalidConfiguration;
+  if (threads == 128) batch_tma_nt<T, 128>(mem, first, nmem, smem, mc, grid, st);
+  else if (threads == 512) batch_tma_nt<T, 512>(mem, first, nmem, smem, mc, grid, st);
+  else if (threads == 1024) batch_tma_nt<T, 1024>(mem, first, nmem, smem, mc, grid, st);
+  else batch_tma_nt<T, 256>(mem, first, nmem, smem, mc, grid, st);
   return cudaGetLastError();
 }
-template cudaError_t launch_batch_tma<double>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
-template cudaError_t launch_batch_tma<float>(const void*, const long long*, int, size_t, int, int, cudaStream_t);
+template cudaError_t launch_batch_tma<double>(const void*, const long long*, int, size_t, int, int, long long, cudaStream_t);
+template cudaError_t launch_batch_tma<float>(const void*, const long long*, int, size_t, int, int, long long, cudaStream_t);
 
 size_t batch_member_bytes(int precision_fp64) {
   return precision_fp64 ? sizeof(BatchMember<double>) : sizeof(BatchMember<float>);

@@ -45,6 +45,9 @@ long long max_rate_partials(const Dims& d);
 cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf, double* partial,
                             double* out, cudaStream_t st);
 cudaError_t launch_to_fp32(const double* src, float* dst, long long n, cudaStream_t st);
+cudaError_t launch_ucfl(const Dims& d, const Grid& g, double dt, const double* const* vel,
+                        const double* const* vlo, double* const* uc, double* const* ucl,
+                        cudaStream_t st);
 cudaError_t launch_lam_combine(const double* lx, const double* ly, const double* lz, int ux, int uy,
                                int uz, float* dst, long long n, cudaStream_t st);
 // step kernel variants: the plane-tiled kernel (rt_step2.cuh) and the
@@ -53,14 +56,17 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_PLANE 0
 #define RT_VARIANT_CELL 1
 #define RT_VARIANT_TMA 2
+#define RT_VARIANT_GROUP 3
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule
-  int threads = 256;  // CTA size of the plane kernel (128, 256, 512)
+  int threads = 512;  // CTA size of the plane kernels (128, 256, 512)
   int sweep = 0;      // 0: bands over m, 1: bands over l
+  int group = 0;      // z planes per item of the group kernel (0: from the CTA size)
 };
 struct PlaneSched;
 PlaneSched make_sched(const Dims& d, const StepTuning& tn);
+PlaneSched make_sched(const Dims& d, const StepTuning& tn, int gz);
 long long sched_items(const Dims& d, const PlaneSched& S);
 template <class T>
 bool plane_ok(const Dims& d);
@@ -71,14 +77,22 @@ template <class T>
 cudaError_t launch_batch(const void* members, const long long* first, int nmem, size_t smem,
                          int threads, int grid, cudaStream_t st);
 template <class T>
-int batch_blocks_per_sm(int threads, size_t smem, bool tma);
+int batch_blocks_per_sm(int threads, size_t smem, bool tma, bool group = false);
+// group kernel: z planes per item for a CTA of `threads` (0 if the kernel cannot run)
+template <class T>
+int group_size(const Dims& d, const StepTuning& tn);
+template <class T>
+size_t group_path_smem(const Dims& d, int G);
+template <class T>
+cudaError_t launch_batch_group(const void* members, const long long* first, int nmem, size_t smem,
+                               int threads, int grid, cudaStream_t st);
 template <class T>
 bool tma_path_ok(const Dims& d);
 template <class T>
 size_t tma_path_smem(const Dims& d);
 template <class T>
 cudaError_t launch_batch_tma(const void* members, const long long* first, int nmem, size_t smem,
-                             int threads, int grid, cudaStream_t st);
+                             int threads, int grid, long long max_nxy, cudaStream_t st);
 size_t batch_member_bytes(int precision_fp64);
 template <class T>
 cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st);

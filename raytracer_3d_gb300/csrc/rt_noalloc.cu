@@ -125,6 +125,7 @@ int rt_max_rate_noalloc(const rt_dims* dims, const double* const* vel, const dou
     st *= nn[a];
   }
   d.ncell = st;
+  fill_plane_strides(d);
   if (d.ncell > RT_NOALLOC_MAX_CELLS)
     return noalloc_fail(RT_ERR_ARG,
                         "rt_max_rate_noalloc: " + std::to_string(d.ncell) +

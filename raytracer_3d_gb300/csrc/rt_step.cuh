@@ -27,6 +27,22 @@ __device__ __forceinline__ double flux_fp64(double v, double dgrid, double dt, d
   return dsub(adv, dif);
 }
 
+// The same flux with uCFL = |v*dt/d(f)| given: uCFL is a constant of the
+// face (velocity, grid, dt), so the binary64 form computes it once, in the
+// reference's operation order, and reuses it every step.
+__device__ __forceinline__ double flux_fp64u(double v, double uCFL, double Ea, double Eb, double Ec,
+                                             double Ed) {
+  const double Rjp = dsub(Ed, Ec);
+  const double Rj = dsub(Ec, Eb);
+  const double Rjm = dsub(Eb, Ea);
+  const double up = v > 0 ? Rjm : Rjp;
+  double Cr = (Rj != 0.0) ? ddiv(up, Rj) : dmul(up, RT_LIT_1E20);
+  Cr = fmax2(0.0, fmax2(fmin2(1.0, dmul(2.0, Cr)), fmin2(2.0, Cr)));
+  const double adv = dmul(dmul(v, dadd(Ec, Eb)), 0.5);
+  const double dif = dmul(dmul(dmul(fabs(v), dadd(dsub(1.0, Cr), dmul(uCFL, Cr))), Rj), 0.5);
+  return dsub(adv, dif);
+}
+
 // ---- binary32 precision form -------------------------------------------
 // Same flux with the limiter written without a division: for Rj != 0,
 // phi(r)*Rj with r = up/Rj equals s*max(0, min(|Rj|, 2t), min(2|Rj|, t)),
@@ -64,6 +80,8 @@ struct StepArgs {
   const T* vel[6];     // right-face velocities
   const T* vlo[6];     // face-0 planes
   const T* lam[3];     // fp64: lambda_x/y/z; fp32: lam[0] = combined rate
+  const T* uc[6];      // fp64: cached |v*dt/d| of the right faces (fp32: unused)
+  const T* ucl[6];     // fp64: the same on the face-0 planes
   double dt;
   int* status;         // device flag: bit 0 = a bounded wait timed out
 };

@@ -70,7 +70,8 @@ struct PlaneSched {
   int band;          // values per band of the banded axis
   int nband;         // ceil(n_banded / band)
   int sweep;         // 0: bands over m, 1: bands over l
-  long long nunits;  // nz * nk
+  int gz;            // z planes per item (1 for the plane kernels)
+  long long nunits;  // ceil(nz / gz) * nk
 };
 
 // Update one work item (one (z,k) plane at one (l,m)) of the band-ordered

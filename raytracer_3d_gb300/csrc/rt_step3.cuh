@@ -74,10 +74,26 @@ template <class T>
 __host__ __device__ __forceinline__ bool tma_ok(const Dims& d) {
   return ((long long)d.n[0] * d.n[1] * (long long)sizeof(T)) % 16 == 0;
 }
+// per-item values that every thread needs, computed by thread 0 while it
+// issues the copies and published through shared memory
+template <class T>
+struct ItemDesc {
+  long long vloff[6];     // offset of the left-face velocities of (x,y)=(0,0), axes 2..5
+  T kcfl_r[6], kinv_r[6], kcfl_l[6];   // binary32 grid constants of the two faces
+  double d_r[6], d_l[6];               // binary64 grid spacings of the two faces
+};
+// shared-memory bytes of the descriptor, rounded to the 16-byte alignment of
+// the planes that follow it
+template <class T>
+__host__ __device__ constexpr size_t desc_bytes() { return (sizeof(ItemDesc<T>) + 15) / 16 * 16; }
+
 template <class T>
 __host__ __device__ __forceinline__ size_t tma_smem(const Dims& d) {
-  return 16 + (size_t)(RT_NPLANE + 2) * d.n[0] * d.n[1] * sizeof(T);
+  return 16 + desc_bytes<T>() + (size_t)(RT_NPLANE + 2) * d.n[0] * d.n[1] * sizeof(T);
 }
+
+// most cells one thread owns in the TMA kernels
+#define RT_TMA_MAXC 4
 
 // coordinate of a neighbour plane after the boundary maps (same rules as
 // map_coord); returns the plane's linear offset
@@ -95,15 +111,57 @@ __device__ __forceinline__ long long nb_plane(const Dims& d, const int c[6], int
   return p;
 }
 
-// returns false only when a bounded wait timed out (status raised)
-template <class T, int NT>
+// grid constants of one face: binary32 form keeps dt/d and 1/d, binary64
+// keeps d (the reference divides)
+template <class T> struct FaceK;
+template <> struct FaceK<float> {
+  float cfl, inv;
+  __device__ __forceinline__ void load(const StepArgs<float>& A, int a, int F, bool with_inv) {
+    cfl = A.t32.cfl[a][pidx(F)];
+    inv = with_inv ? A.t32.inv_d[a][pidx(F)] : 0.f;
+  }
+};
+template <> struct FaceK<double> {
+  double d;
+  __device__ __forceinline__ void load(const StepArgs<double>& A, int a, int F, bool) {
+    d = A.g.d[a][pidx(F)];
+  }
+};
+// u: the cached uCFL of the face (binary64 form); the binary32 form forms
+// |v|*dt/d from its table instead
+__device__ __forceinline__ float kflux(const StepArgs<float>&, const FaceK<float>& k, float v, float,
+                                       float Ea, float Eb, float Ec, float Ed) {
+  return flux_fp32(v, k.cfl, Ea, Eb, Ec, Ed);
+}
+__device__ __forceinline__ double kflux(const StepArgs<double>&, const FaceK<double>&, double v,
+                                        double u, double Ea, double Eb, double Ec, double Ed) {
+  return flux_fp64u(v, u, Ea, Eb, Ec, Ed);
+}
+// cached uCFL of the binary64 form (zero for binary32, where it is unused)
+template <class T>
+__device__ __forceinline__ T ucfl_at(const T* base, long long i) {
+  if constexpr (sizeof(T) == 8) return base[i];
+  else return T(0);
+}
+// dE -= (fr - fl)/d with the right face's constants
+__device__ __forceinline__ float kdiv(const FaceK<float>& kr, float dE, float fr, float fl) {
+  return dE - (fr - fl) * kr.inv;
+}
+__device__ __forceinline__ double kdiv(const FaceK<double>& kr, double dE, double fr, double fl) {
+  return dsub(dE, ddiv(dsub(fr, fl), kr.d));
+}
+
+// Update one work item.  MAXC = most cells one thread owns (nx*ny <= MAXC*NT).
+// Returns false only when a bounded wait timed out (status raised).
+template <class T, int NT, int MAXC>
 __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched& S, long long item,
                                          unsigned char* smem_raw, uint32_t phase) {
   const Dims& d = A.d;
   const int nx = d.n[0], ny = d.n[1], nz = d.n[2], nl = d.n[4], nm = d.n[5];
   const int nxy = nx * ny;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-  T* sP = reinterpret_cast<T*>(smem_raw + 16);   // RT_NPLANE planes
+  ItemDesc<T>* desc = reinterpret_cast<ItemDesc<T>*>(smem_raw + 16);
+  T* sP = reinterpret_cast<T*>(smem_raw + 16 + desc_bytes<T>());   // RT_NPLANE planes
   T* sFx = sP + (size_t)RT_NPLANE * nxy;
   T* sFy = sFx + nxy;
 
@@ -146,84 +204,146 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
       slot += 4;
     }
   }
-  // uniform per-CTA data while the copies fly
-  const T* vlft[6];
-  long long vlft_off[6];
+
+  // ---- while the copies fly: thread 0 fills the item descriptor ----
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int a = 2; a < 6; a++) {
-    if (c[a] > 0) { vlft[a] = A.vel[a]; vlft_off[a] = p0 - d.s[a]; }
-    else {  // face 0 plane: (x,y) contiguous at the plane index of (0,0,c[2..5])
-      long long q = 0;
-      for (int bb = 2; bb < 6; bb++) q += (long long)c[bb] * plane_stride(d, a, bb);
-      vlft[a] = A.vlo[a];
-      vlft_off[a] = q;
+    for (int a = 2; a < 6; a++) {
+      long long off;
+      if (c[a] > 0) {
+        off = p0 - d.s[a];
+      } else {  // face-0 plane: (x,y) contiguous at the plane index of (0,0,c[2..5])
+        off = 0;
+        for (int bb = 2; bb < 6; bb++) off += (long long)c[bb] * plane_stride(d, a, bb);
+      }
+      desc->vloff[a] = off;
+      if (d.n[a] > 1) {
+        if constexpr (sizeof(T) == 4) {
+          desc->kcfl_r[a] = A.t32.cfl[a][pidx(c[a] + 1)];
+          desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
+          desc->kcfl_l[a] = A.t32.cfl[a][pidx(c[a])];
+        } else {
+          desc->d_r[a] = A.g.d[a][pidx(c[a] + 1)];
+          desc->d_l[a] = A.g.d[a][pidx(c[a])];
+        }
+      }
     }
   }
+  __syncthreads();
+  FaceK<T> kr[6], kl[6];
+  long long vloff[6];
+#pragma unroll
+  for (int a = 2; a < 6; a++) {
+    vloff[a] = desc->vloff[a];
+    if constexpr (sizeof(T) == 4) {
+      kr[a].cfl = desc->kcfl_r[a];
+      kr[a].inv = desc->kinv_r[a];
+      kl[a].cfl = desc->kcfl_l[a];
+      kl[a].inv = 0.f;
+    } else {
+      kr[a].d = desc->d_r[a];
+      kl[a].d = desc->d_l[a];
+    }
+  }
+  // q -> (x, y) by multiplying with ceil(2^32/nx): exact for q*nx <= 2^32,
+  // which holds because nx*ny <= 4096 on this path
+  const unsigned long long ymul = ((1ull << 32) + (unsigned)nx - 1) / (unsigned)nx;
 
   if (!mbar_wait_bounded(bar, phase, A.status)) return false;
 
   const T* sE = sP;
   // ---- x and y right-face fluxes, once per face ----
-  for (int q = threadIdx.x; q < nxy; q += NT) {
-    const int y = q / nx, x = q - y * nx;
-    if (nx > 1) {
-      const int r = y * nx;
-      const int xm = x > 0 ? x - 1 : 0, xp = x + 1 < nx ? x + 1 : nx - 1,
-                xpp = x + 2 < nx ? x + 2 : nx - 1;
-      const T v = ld_stream(A.vel[0] + p0 + q);
-      sFx[q] = face_flux<T>(A, 0, x + 1, v, sE[r + xm], sE[q], sE[r + xp], sE[r + xpp]);
-    }
-    if (ny > 1) {
-      const int ym = y > 0 ? y - 1 : 0, yp = y + 1 < ny ? y + 1 : ny - 1,
-                ypp = y + 2 < ny ? y + 2 : ny - 1;
-      const T v = ld_stream(A.vel[1] + p0 + q);
-      sFy[q] = face_flux<T>(A, 1, y + 1, v, sE[ym * nx + x], sE[q], sE[yp * nx + x], sE[ypp * nx + x]);
+#pragma unroll 1
+  for (int j = 0; j < MAXC; j++) {
+    const int q = threadIdx.x + j * NT;
+    if (q < nxy) {
+      const int y = (int)(((unsigned long long)q * ymul) >> 32), x = q - y * nx;
+      if (nx > 1) {
+        const int r = y * nx;
+        const int xm = x > 0 ? x - 1 : 0, xp = x + 1 < nx ? x + 1 : nx - 1,
+                  xpp = x + 2 < nx ? x + 2 : nx - 1;
+        FaceK<T> kx;
+        kx.load(A, 0, x + 1, false);
+        sFx[q] = kflux(A, kx, ld_stream(A.vel[0] + p0 + q), ucfl_at<T>(A.uc[0], p0 + q), sE[r + xm], sE[q],
+                       sE[r + xp], sE[r + xpp]);
+      }
+      if (ny > 1) {
+        const int ym = y > 0 ? y - 1 : 0, yp = y + 1 < ny ? y + 1 : ny - 1,
+                  ypp = y + 2 < ny ? y + 2 : ny - 1;
+        FaceK<T> ky;
+        ky.load(A, 1, y + 1, false);
+        sFy[q] = kflux(A, ky, ld_stream(A.vel[1] + p0 + q), ucfl_at<T>(A.uc[1], p0 + q), sE[ym * nx + x],
+                       sE[q], sE[yp * nx + x], sE[ypp * nx + x]);
+      }
     }
   }
   __syncthreads();
 
   // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
-  for (int q = threadIdx.x; q < nxy; q += NT) {
-    const int y = q / nx, x = q - y * nx;
-    const long long p = p0 + q;
-    const T e0 = sE[q];
-    T dE = T(0);
-    if (nx > 1) {
-      const T fl = x > 0 ? sFx[q - 1] : open_face0_flux<T>(A.vlo[0][p0 / nx + y], e0);
-      dE = div_acc<T>(A, 0, x + 1, dE, sFx[q], fl);
-    }
-    if (ny > 1) {
-      const T fl = y > 0 ? sFy[q - nx] : open_face0_flux<T>(A.vlo[1][p0 / ny + x], e0);
-      dE = div_acc<T>(A, 1, y + 1, dE, sFy[q], fl);
-    }
+#pragma unroll 1
+  for (int j = 0; j < MAXC; j++) {
+    const int q = threadIdx.x + j * NT;
+    if (q < nxy) {
+      const int y = (int)(((unsigned long long)q * ymul) >> 32), x = q - y * nx;
+      // the cell's face velocities and rate, loaded together
+      T vr[4], vl[4], ur[4], ul[4];
 #pragma unroll
-    for (int a = 2; a < 6; a++) {
-      if (d.n[a] <= 1) continue;
-      const T* sN = sP + (size_t)(1 + 4 * (a - 2)) * nxy;
-      const T Em2 = sN[q], Em1 = sN[nxy + q], Ep1 = sN[2 * nxy + q], Ep2 = sN[3 * nxy + q];
-      const T vr = A.vel[a][p];
-      const T vl = vlft[a][vlft_off[a] + q];
-      const T fr = face_flux<T>(A, a, c[a] + 1, vr, Em1, e0, Ep1, Ep2);
-      const T fl = face_flux<T>(A, a, c[a], vl, Em2, Em1, e0, Ep1);
-      dE = div_acc<T>(A, a, c[a] + 1, dE, fr, fl);
-    }
-    if constexpr (sizeof(T) == 8) {
-      double mf = 0.;
-      if (nx > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[0] + p)));
-      if (ny > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[1] + p)));
-      if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p)));
-      st_stream(A.Enew + p, dadd(e0, dmul(A.dt, dsub(dE, mf))));
-    } else {
-      const T mf = e0 * ld_stream(A.lam[0] + p);
-      st_stream(A.Enew + p, (T)(e0 + (T)A.dt * (dE - mf)));
+      for (int a = 2; a < 6; a++) {
+        const bool act = d.n[a] > 1;
+        vr[a - 2] = act ? A.vel[a][p0 + q] : T(0);
+        vl[a - 2] = act ? (c[a] > 0 ? A.vel[a][vloff[a] + q] : A.vlo[a][vloff[a] + q]) : T(0);
+        ur[a - 2] = act ? ucfl_at<T>(A.uc[a], p0 + q) : T(0);
+        ul[a - 2] = act ? (c[a] > 0 ? ucfl_at<T>(A.uc[a], vloff[a] + q) : ucfl_at<T>(A.ucl[a], vloff[a] + q))
+                        : T(0);
+      }
+      const T e0 = sE[q];
+      T dE = T(0);
+      if (nx > 1) {
+        FaceK<T> kx;
+        kx.load(A, 0, x + 1, true);
+        const T fl = x > 0 ? sFx[q - 1] : open_face0_flux<T>(A.vlo[0][p0 / nx + y], e0);
+        dE = kdiv(kx, dE, sFx[q], fl);
+      }
+      if (ny > 1) {
+        FaceK<T> ky;
+        ky.load(A, 1, y + 1, true);
+        const T fl = y > 0 ? sFy[q - nx] : open_face0_flux<T>(A.vlo[1][p0 / ny + x], e0);
+        dE = kdiv(ky, dE, sFy[q], fl);
+      }
+#pragma unroll
+      for (int a = 2; a < 6; a++) {
+        if (d.n[a] <= 1) continue;
+        const T* sN = sP + (size_t)(1 + 4 * (a - 2)) * nxy;
+        const T Em2 = sN[q], Em1 = sN[nxy + q], Ep1 = sN[2 * nxy + q], Ep2 = sN[3 * nxy + q];
+        const T fr = kflux(A, kr[a], vr[a - 2], ur[a - 2], Em1, e0, Ep1, Ep2);
+        const T fl = kflux(A, kl[a], vl[a - 2], ul[a - 2], Em2, Em1, e0, Ep1);
+        dE = kdiv(kr[a], dE, fr, fl);
+      }
+      if constexpr (sizeof(T) == 8) {
+        // meanfl = ((0 + E*lx) + E*ly) + E*lz, integrate.f90:202-252
+        double mf = 0.;
+        if (nx > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[0] + p0 + q)));
+        if (ny > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[1] + p0 + q)));
+        if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p0 + q)));
+        st_stream(A.Enew + p0 + q, dadd(e0, dmul(A.dt, dsub(dE, mf))));
+      } else {
+        const T mf = e0 * ld_stream(A.lam[0] + p0 + q);
+        st_stream(A.Enew + p0 + q, (T)(e0 + (T)A.dt * (dE - mf)));
+      }
     }
   }
   __syncthreads();  // shared memory and the barrier are reused by the next item
   return true;
 }
 
+// registers are left to the compiler (a cap of 64 made the binary32 kernel
+// spill and run slower)
 template <class T, int NT>
-__global__ void __launch_bounds__(NT) step_tma_kernel(StepArgs<T> A, PlaneSched S) {
+struct TmaMinBlocks { static constexpr int value = 1; };
+
+template <class T, int NT, int MAXC>
+__global__ void __launch_bounds__(NT, (TmaMinBlocks<T, NT>::value))
+    step_tma_kernel(StepArgs<T> A, PlaneSched S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   if (threadIdx.x == 0) {
@@ -231,13 +351,14 @@ __global__ void __launch_bounds__(NT) step_tma_kernel(StepArgs<T> A, PlaneSched 
     fence_mbar_init();
   }
   __syncthreads();
-  tma_item<T, NT>(A, S, blockIdx.x, smem_raw, 0);
+  tma_item<T, NT, MAXC>(A, S, blockIdx.x, smem_raw, 0);
 }
 
 // persistent batched form: the mbarrier is re-armed for every item, the
 // phase bit alternates
-template <class T, int NT>
-__global__ void __launch_bounds__(NT) batch_tma_kernel(const BatchMember<T>* __restrict__ mem,
+template <class T, int NT, int MAXC>
+__global__ void __launch_bounds__(NT, (TmaMinBlocks<T, NT>::value))
+    batch_tma_kernel(const BatchMember<T>* __restrict__ mem,
                                                        const long long* __restrict__ first,
                                                        int nmem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -258,7 +379,7 @@ __global__ void __launch_bounds__(NT) batch_tma_kernel(const BatchMember<T>* __r
     const long long per = (long long)M.S.nunits * M.S.band * (M.S.sweep ? M.A.d.n[5] : M.A.d.n[4]);
     const int banded = (int)(ii / per) * M.S.band + (int)((ii / M.S.nunits) % M.S.band);
     if (banded >= (M.S.sweep ? M.A.d.n[4] : M.A.d.n[5])) continue;
-    if (!tma_item<T, NT>(M.A, M.S, ii, smem_raw, phase)) return;
+    if (!tma_item<T, NT, MAXC>(M.A, M.S, ii, smem_raw, phase)) return;
     phase ^= 1;
   }
 }

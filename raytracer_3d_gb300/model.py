@@ -162,9 +162,9 @@ class Model:
         return {k: getattr(b, k) for k in _lib.BUDGET_FIELDS}, arrs
 
     # ---- plumbing ---------------------------------------------------------------
-    VARIANTS = {"plane": 0, "cell": 1, "tma": 2}
+    VARIANTS = {"plane": 0, "cell": 1, "tma": 2, "group": 3}
 
-    def set_tuning(self, variant="tma", band=8, threads=256, sweep=0):
+    def set_tuning(self, variant="tma", band=8, threads=512, sweep=0):
         """Schedule of the step kernel; never changes results."""
         self._check(self._lib.rt_set_tuning(self._h, self.VARIANTS[variant], int(band), int(threads)),
                     "rt_set_tuning")

@@ -18,7 +18,6 @@ Latency of a request = completion time - arrival time.  The executor is
 pluggable so the scheduling logic is testable without a GPU
 (`FakeExecutor`).
 """
-import heapq
 import math
 import time
 from dataclasses import dataclass, field
@@ -99,63 +98,98 @@ class ServeReport:
 
 
 class Server:
-    def __init__(self, executor, budget_bytes=120e9, chunk_max=50, max_members=64):
+    """Continuous-batching request loop.  With an executor whose
+    `overlap_setup` is true, set-up of admitted requests (`admit_async`) runs
+    in a background thread pool while chunks run on the GPU; new members join
+    at the next chunk boundary once their set-up has finished."""
+
+    def __init__(self, executor, budget_bytes=120e9, chunk_max=50, max_members=64, setup_workers=2):
         self.ex = executor
         self.budget = float(budget_bytes)
         self.chunk_max = int(chunk_max)
         self.max_members = int(max_members)
+        self.setup_workers = int(setup_workers)
 
     def run(self, requests):
         ex = self.ex
+        asynchronous = getattr(ex, "overlap_setup", False)
+        pool = None
+        if asynchronous:
+            import concurrent.futures as cf
+            pool = cf.ThreadPoolExecutor(self.setup_workers)
         queue = sorted(requests, key=lambda r: r.arrival)
         qi = 0
-        active = []            # (request, member, remaining)
-        used = 0.0
+        active = []            # [request, member, remaining]
+        pending = []           # [request, future]
+        used = 0.0             # resident bytes of admitted requests
+        transient = 0.0        # set-up bytes of requests still being set up
         peak = 0.0
         chunks = 0
         backlog_max = 0
         total = 0
         timeline = []
         t0 = ex.now()
-        while qi < len(queue) or active:
-            now = ex.now() - t0
-            # ---- admission (arrival order, HBM budget) ----
-            while qi < len(queue) and queue[qi].arrival <= now and len(active) < self.max_members:
-                r = queue[qi]
-                need_res, need_tmp = ex.footprint(r)
-                if need_res + need_tmp > self.budget:
-                    raise ValueError("request %d needs %.3g B, more than the whole budget" % (r.rid, need_res + need_tmp))
-                if used + need_res + need_tmp > self.budget:
-                    break                                    # wait for memory to free up
-                member = ex.admit(r)                         # overlaps the running chunk
-                r.admitted = ex.now() - t0
-                used += need_res
-                peak = max(peak, used + need_tmp)
-                active.append([r, member, r.steps])
-                qi += 1
-            backlog = sum(1 for r in queue[qi:] if r.arrival <= now)
-            backlog_max = max(backlog_max, backlog)
-            if not active:
-                # idle until the next arrival
-                ex.wait_until(t0 + queue[qi].arrival)
-                continue
-            # ---- one chunk for all active members ----
-            n = min(self.chunk_max, min(a[2] for a in active))
-            ex.step([a[1] for a in active], n)
-            chunks += 1
-            total += n * sum(a[0].cells for a in active)
-            for a in active:
-                a[2] -= n
-            done = [a for a in active if a[2] == 0]
-            if done:
-                ex.sync()
-                for a in done:
-                    r = a[0]
-                    r.result = ex.retire(a[1])
-                    r.finished = ex.now() - t0
-                    used -= ex.footprint(r)[0]
-                active = [a for a in active if a[2] > 0]
-            timeline.append((ex.now() - t0, len(active), used))
+        try:
+            while qi < len(queue) or active or pending:
+                now = ex.now() - t0
+                # ---- admission (arrival order, HBM budget) ----
+                while (qi < len(queue) and queue[qi].arrival <= now
+                       and len(active) + len(pending) < self.max_members):
+                    r = queue[qi]
+                    need_res, need_tmp = ex.footprint(r)
+                    if need_res + need_tmp > self.budget:
+                        raise ValueError("request %d needs %.3g B, more than the whole budget"
+                                         % (r.rid, need_res + need_tmp))
+                    if used + transient + need_res + need_tmp > self.budget:
+                        break                                    # wait for memory to free up
+                    r.admitted = ex.now() - t0
+                    used += need_res
+                    if asynchronous:
+                        transient += need_tmp
+                        pending.append([r, pool.submit(ex.admit_async, r)])
+                    else:
+                        member = ex.admit(r)
+                        active.append([r, member, r.steps])
+                    peak = max(peak, used + transient + (0 if asynchronous else need_tmp))
+                    qi += 1
+                # ---- set-ups that finished join the batch ----
+                still = []
+                for r, fut in pending:
+                    if fut.done():
+                        active.append([r, fut.result(), r.steps])
+                        transient -= ex.footprint(r)[1]
+                    else:
+                        still.append([r, fut])
+                pending = still
+                backlog = sum(1 for r in queue[qi:] if r.arrival <= now)
+                backlog_max = max(backlog_max, backlog)
+                if not active:
+                    if pending:
+                        import concurrent.futures as cf
+                        cf.wait([f for _, f in pending], return_when=cf.FIRST_COMPLETED)
+                    elif qi < len(queue):
+                        ex.wait_until(t0 + queue[qi].arrival)
+                    continue
+                # ---- one chunk for all active members ----
+                n = min(self.chunk_max, min(a[2] for a in active))
+                ex.step([a[1] for a in active], n)
+                chunks += 1
+                total += n * sum(a[0].cells for a in active)
+                for a in active:
+                    a[2] -= n
+                done = [a for a in active if a[2] == 0]
+                if done:
+                    ex.sync()
+                    for a in done:
+                        r = a[0]
+                        r.result = ex.retire(a[1])
+                        r.finished = ex.now() - t0
+                        used -= ex.footprint(r)[0]
+                    active = [a for a in active if a[2] > 0]
+                timeline.append((ex.now() - t0, len(active), used))
+        finally:
+            if pool is not None:
+                pool.shutdown(wait=True)
         makespan = ex.now() - t0
         return ServeReport(queue, makespan, total, int(peak), chunks, backlog_max, timeline)
 
@@ -163,6 +197,8 @@ class Server:
 class GpuExecutor:
     """Members are `Model`s of libraytracer_gb300.so; a chunk is one
     `Batch.integrate` (persistent, graph-captured launches)."""
+
+    overlap_setup = True   # Server runs admit_async in worker threads
 
     def __init__(self, precision="fp32", tune=False, batch_tuning=None):
         self.precision = precision
@@ -186,6 +222,11 @@ class GpuExecutor:
     def admit(self, r):
         from .configs import build_model
         return build_model(r.exp, self.precision)
+
+    def admit_async(self, r):
+        """set-up in a worker thread: numpy work and the library calls
+        release the interpreter lock, so it overlaps the running chunk"""
+        return self.admit(r)
 
     def step(self, members, n):
         from .batch import Batch
@@ -218,6 +259,8 @@ class GpuExecutor:
 
 class SequentialExecutor(GpuExecutor):
     """Baseline: one request at a time, each stepped alone (rt_integrate)."""
+
+    overlap_setup = False  # set-up inline: no overlap in the baseline
 
     def step(self, members, n):
         for m in members:

@@ -20,7 +20,7 @@ def _members(count, seed, steps=7, spatial=(4, 6, 8), spectral=(4, 6, 8)):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-@pytest.mark.parametrize("tuning", [(8, 256, 0, 16), (3, 128, 1, 2), (1, 512, 0, 4)])
+@pytest.mark.parametrize("tuning", [(8, 256, 0, 16), (3, 128, 1, 2), (1, 512, 0, 4), (4, 1024, 1, 6)])
 def test_batch_equals_members_alone(precision, tuning):
     from raytracer_3d_gb300.batch import Batch
     exps = _members(6, seed=11)

@@ -66,8 +66,9 @@ def test_coefficients_bit_identical(name):
         m.close()
 
 
-SCHEDULES = [("tma", 8, 256, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plane", 8, 256, 0),
-             ("plane", 2, 512, 1), ("cell", 8, 256, 0)]
+SCHEDULES = [("tma", 8, 1024, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plane", 8, 256, 0),
+             ("plane", 2, 512, 1), ("group", 8, 256, 0), ("group", 3, 1024, 1), ("group", 2, 128, 0),
+             ("cell", 8, 256, 0)]
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -170,13 +171,13 @@ def test_fp32_schedules_agree():
         m.integrate(5)
         outs.append(m.get_state().copy())
         m.close()
-    for o in outs[1:5]:
+    for o in outs[1:8]:
         assert np.array_equal(o, outs[0])
     # the cell kernel may contract multiply-adds differently
-    assert max_rel(outs[5], outs[0]) < 1e-6
+    assert max_rel(outs[8], outs[0]) < 1e-6
 
 
-@pytest.mark.parametrize("variant", ["tma", "plane", "cell"])
+@pytest.mark.parametrize("variant", ["tma", "group", "plane", "cell"])
 def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
     after 200 steps of the all-axes shear case."""
