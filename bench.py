@@ -176,8 +176,9 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-FP32_CANDIDATES = [(v, b, t, s) for v in ("tma", "group") for t in (256, 512, 1024) for b in (4, 8)
-                   for s in (0, 1)]
+FP32_CANDIDATES = ([(v, b, t, s) for v in ("ws", "wsd") for t in (128, 256, 512) for b in (4, 8) for s in (0, 1)]
+                   + [(v, b, t, s) for v in ("pipe", "tma") for t in (256, 512, 1024) for b in (4, 8)
+                      for s in (0, 1)])
 
 
 def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False):
@@ -305,13 +306,16 @@ def roofline(precision, cells, seconds_per_launch):
 
 def gpu_arm(args):
     rank, world, local, dist = dist_init(args.gpus)
-    n = (args.n,) * 6
+    n = tuple(int(v) for v in args.dims.split(",")) if args.dims else (args.n,) * 6
     sched = (args.variant, args.band, args.threads, args.sweep)
     if args.no_fp64:  # profiling runs of the fp32 form only
         f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
         if rank == 0:
-            print(json.dumps({"profile_only": "fp32", "cells": f32["cells"],
-                              "ms_per_step": 1e3 * f32["seconds"] / args.steps}), flush=True)
+            ms = 1e3 * f32["seconds"] / args.steps
+            print(json.dumps({"profile_only": "fp32", "dims": n, "cells": f32["cells"], "ms_per_step": ms,
+                              "cells_per_s": f32["cells"] / (ms / 1e3),
+                              "schedule": f32["schedule"], "tuning_table_ms": f32["tuning_table_ms"],
+                              "roofline": roofline("fp32", f32["cells"], ms / 1e3)}), flush=True)
         return
     # the binary64 form is bound by the FP64 pipe; 256-thread CTAs keep its
     # registers unspilled (the flags set the fp32 schedule when --tune 0)
@@ -385,7 +389,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
-    ap.add_argument("--variant", default="tma", choices=("tma", "group", "plane", "cell"))
+    ap.add_argument("--dims", default=None, help="nx,ny,nz,nk,nl,nm of a profiling case (with --no-fp64)")
+    ap.add_argument("--variant", default="tma", choices=("ws", "wsd", "pipe", "tma", "group", "plane", "cell"))
     ap.add_argument("--band", type=int, default=8)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--sweep", type=int, default=0)

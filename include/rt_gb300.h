@@ -139,9 +139,16 @@ int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int,
 /* Schedule of the step kernel (no effect on results).  variant: 2 = plane
  * tiled with bulk-copy (TMA) staging of the E planes (default; used when a
  * plane of E is a multiple of 16 bytes), 3 = the same with several z planes
- * per work item (for small x-y planes), 0 = plane tiled with plain loads,
- * 1 = one thread per cell; band: values per band of the plane schedule
- * (default 8); threads: CTA size 128, 256, 512 or 1024 (default 512).  Chosen by the autotuner
+ * per work item (for small x-y planes), 4 = persistent CTAs that stage the
+ * next item while computing the current one, 5 = persistent CTAs with one
+ * producer warp feeding a ring of 2-4 staged items to `threads` consumer
+ * threads that load the next item's velocities ahead, 6 = as 5 with the
+ * velocities loaded at the start of each item (4-6: binary32 form; binary64
+ * uses variant 2), 0 = plane tiled with plain loads, 1 = one thread per
+ * cell; band: values per band of the plane schedule (default 8); threads:
+ * CTA size 128, 256, 512 or 1024 (default 512; consumer threads of
+ * variants 5 and 6: 128, 256 or 512).  Shapes a variant cannot run fall
+ * back to the next one that can.  Chosen by the autotuner
  * (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);
 /* Sweep order of the plane schedule: 0 = bands over m (default), 1 = bands

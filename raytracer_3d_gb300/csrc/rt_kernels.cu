@@ -622,6 +622,11 @@ static cudaError_t launch_group_nt(const StepArgs<T>& A, const PlaneSched& S, lo
 
 template <class T>
 cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st) {
+  if constexpr (sizeof(T) == 4) {
+    bool done = false;
+    cudaError_t e = launch_persist(A, tn, st, done);
+    if (done) return e;
+  }
   if (tn.variant == RT_VARIANT_GROUP) {
     const int G = group_size<T>(A.d, tn);
     if (G > 0) {
@@ -633,7 +638,9 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
       return launch_group_nt<T, 256>(A, S, nblk, st);
     }
   }
-  if (tn.variant == RT_VARIANT_TMA && tma_path_ok<T>(A.d) &&
+  if ((tn.variant == RT_VARIANT_TMA || tn.variant == RT_VARIANT_PIPE || tn.variant == RT_VARIANT_WS ||
+       tn.variant == RT_VARIANT_WSD) &&
+      tma_path_ok<T>(A.d) &&
       tma_maxc((long long)A.d.n[0] * A.d.n[1], tn.threads) <= RT_TMA_MAXC) {
     const PlaneSched S = make_sched(A.d, tn);
     const long long nblk = sched_items(A.d, S);
@@ -642,7 +649,9 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
     if (tn.threads == 1024) return launch_tma_nt<T, 1024>(A, S, nblk, st);
     return launch_tma_nt<T, 256>(A, S, nblk, st);
   }
-  if ((tn.variant == RT_VARIANT_PLANE || tn.variant == RT_VARIANT_TMA) && plane_ok<T>(A.d)) {
+  if ((tn.variant == RT_VARIANT_PLANE || tn.variant == RT_VARIANT_TMA || tn.variant == RT_VARIANT_PIPE ||
+       tn.variant == RT_VARIANT_GROUP || tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) &&
+      plane_ok<T>(A.d)) {
     const PlaneSched S = make_sched(A.d, tn);
     const long long nblk = sched_items(A.d, S);
     const size_t sm = plane_smem<T>(A.d);

@@ -57,6 +57,9 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_CELL 1
 #define RT_VARIANT_TMA 2
 #define RT_VARIANT_GROUP 3
+#define RT_VARIANT_PIPE 4
+#define RT_VARIANT_WS 5
+#define RT_VARIANT_WSD 6
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule
@@ -96,6 +99,9 @@ cudaError_t launch_batch_tma(const void* members, const long long* first, int nm
 size_t batch_member_bytes(int precision_fp64);
 template <class T>
 cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st);
+// persistent binary32 kernels (rt_persist.cu); done = false when the tuning
+// does not select one of them or the shape does not fit them
+cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);
 DiagSizes diag_sizes(const Dims& d);
 template <class T>
 cudaError_t launch_diag(const StepArgs<T>& A, const T* Ecur, double* scratch, double* vol3,

@@ -1,0 +1,144 @@
+// rt_persist.cu -- launchers of the persistent binary32 step kernels:
+// the two-stage pipelined kernel (rt_step5.cuh, variant RT_VARIANT_PIPE) and
+// the warp-specialised multi-stage kernel (rt_step6.cuh, variants
+// RT_VARIANT_WS with register look-ahead and RT_VARIANT_WSD without).
+// Kept in a translation unit of their own so the library builds in parallel.
+#include <algorithm>
+
+#include "rt_kernels.h"
+#include "rt_step6.cuh"
+
+namespace rt {
+
+namespace {
+
+int most_cells(long long nxy, int nt) { return (int)((nxy + nt - 1) / nt); }
+
+template <class K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int sm_count() {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm;
+}
+
+// one resident wave of persistent CTAs, at most one per item
+template <class K>
+cudaError_t persistent_grid(K kernel, int block, size_t smem, long long nitems, long long& grid) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  grid = std::min<long long>(nitems, (long long)per_sm * sm_count());
+  return cudaSuccess;
+}
+
+// ---- two-stage pipelined kernel ----
+template <int NT, int MAXC>
+cudaError_t launch_pipe_c(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const size_t sm = pipe_smem(A.d);
+  cudaError_t e = set_smem(step_pipe_kernel<NT, MAXC>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d);
+  long long grid = 0;
+  e = persistent_grid(step_pipe_kernel<NT, MAXC>, NT, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_pipe_kernel<NT, MAXC><<<(unsigned)grid, NT, sm, st>>>(A, S, nitems);
+  return cudaGetLastError();
+}
+
+template <int NT>
+cudaError_t launch_pipe_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int mc = most_cells((long long)A.d.n[0] * A.d.n[1], NT);
+  if (mc <= 1) return launch_pipe_c<NT, 1>(A, S, st);
+  if (mc <= 2) return launch_pipe_c<NT, 2>(A, S, st);
+  return launch_pipe_c<NT, 4>(A, S, st);
+}
+
+bool pipe_ok(const Dims& d, int threads) {
+  return tma_ok<float>(d) && pipe_smem(d) <= 220 * 1024 &&
+         most_cells((long long)d.n[0] * d.n[1], threads) <= RT_TMA_MAXC && (long long)d.n[0] * d.n[1] <= 4096;
+}
+
+// ---- warp-specialised multi-stage kernel ----
+// rows per consumer thread: the thread columns are x = t % nx, so NT / nx
+// row chunks of R rows must cover ny
+int ws_rows(const Dims& d, int nt) {
+  const int nyc = nt / d.n[0];
+  if (nyc < 1) return 0;
+  const int R = (d.n[1] + nyc - 1) / nyc;
+  return R <= 1 ? 1 : (R <= 2 ? 2 : (R <= 4 ? 4 : 0));
+}
+int ws_max_smem() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  return v - 1024;
+}
+int ws_stages(const Dims& d) {
+  const long long room = (long long)ws_max_smem() - (long long)ws_head_bytes();
+  const long long per = (long long)ws_stage_bytes(d);
+  const long long ns = room > 0 ? room / per : 0;
+  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
+}
+bool ws_ok(const Dims& d, int threads) {
+  if (threads != 128 && threads != 256 && threads != 512) return false;
+  return d.n[0] >= 2 && d.n[1] >= 2 && tma_ok<float>(d) && d.n[0] <= threads && ws_rows(d, threads) > 0 &&
+         (long long)d.n[0] * d.n[1] <= 4096 && dense_items(d) < (1LL << 31) && ws_stages(d) >= 2;
+}
+
+template <int NT, int R, int PF>
+cudaError_t launch_ws_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int ns = ws_stages(A.d);
+  const size_t sm = ws_smem(A.d, ns);
+  cudaError_t e = set_smem(step_ws_kernel<NT, R, PF>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d);
+  long long grid = 0;
+  e = persistent_grid(step_ws_kernel<NT, R, PF>, NT + 32, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_ws_kernel<NT, R, PF><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
+  return cudaGetLastError();
+}
+
+template <int NT, int PF>
+cudaError_t launch_ws_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int R = ws_rows(A.d, NT);
+  if (R == 1) return launch_ws_r<NT, 1, PF>(A, S, st);
+  if (R == 2) return launch_ws_r<NT, 2, PF>(A, S, st);
+  return launch_ws_r<NT, 4, PF>(A, S, st);
+}
+
+template <int PF>
+cudaError_t launch_ws_pf(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st) {
+  if (threads == 128) return launch_ws_nt<128, PF>(A, S, st);
+  if (threads == 256) return launch_ws_nt<256, PF>(A, S, st);
+  return launch_ws_nt<512, PF>(A, S, st);
+}
+
+}  // namespace
+
+cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
+  done = false;
+  if ((tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) && ws_ok(A.d, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.variant == RT_VARIANT_WS) return launch_ws_pf<1>(A, S, tn.threads, st);
+    return launch_ws_pf<0>(A, S, tn.threads, st);
+  }
+  if (tn.variant == RT_VARIANT_PIPE && pipe_ok(A.d, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.threads == 128) return launch_pipe_nt<128>(A, S, st);
+    if (tn.threads == 512) return launch_pipe_nt<512>(A, S, st);
+    if (tn.threads == 1024) return launch_pipe_nt<1024>(A, S, st);
+    return launch_pipe_nt<256>(A, S, st);
+  }
+  return cudaSuccess;
+}
+
+}  // namespace rt

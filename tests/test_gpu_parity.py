@@ -68,7 +68,8 @@ def test_coefficients_bit_identical(name):
 
 SCHEDULES = [("tma", 8, 1024, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plane", 8, 256, 0),
              ("plane", 2, 512, 1), ("group", 8, 256, 0), ("group", 3, 1024, 1), ("group", 2, 128, 0),
-             ("cell", 8, 256, 0)]
+             ("pipe", 8, 256, 0), ("pipe", 3, 512, 1), ("pipe", 5, 1024, 0), ("ws", 8, 256, 0),
+             ("ws", 3, 512, 1), ("wsd", 4, 128, 0), ("wsd", 8, 512, 1), ("cell", 8, 256, 0)]
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -164,20 +165,44 @@ def _energy(E, o, n):
 def test_fp32_schedules_agree():
     """the schedule never changes the binary32 result"""
     exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
-    outs = []
+    outs = {}
     for sched in SCHEDULES:
         m = configs.build_model(exp, "fp32")
         m.set_tuning(*sched)
         m.integrate(5)
+        outs[sched] = m.get_state().copy()
+        m.close()
+    first = outs[SCHEDULES[0]]
+    for sched, o in outs.items():
+        if sched[0] == "cell":
+            # the cell kernel may contract multiply-adds differently
+            assert max_rel(o, first) < 1e-6
+        else:
+            assert np.array_equal(o, first), sched
+
+
+@pytest.mark.parametrize("n", [(32, 32, 4, 4, 2, 6), (24, 16, 6, 4, 6, 10), (16, 8, 5, 2, 4, 6),
+                               (20, 12, 4, 2, 4, 6), (64, 64, 4, 2, 2, 2)])
+@pytest.mark.parametrize("tuning", [("pipe", 4, 256, 0), ("pipe", 4, 512, 1), ("pipe", 8, 1024, 0),
+                                    ("ws", 4, 128, 0), ("ws", 4, 256, 1), ("ws", 8, 512, 0),
+                                    ("wsd", 4, 128, 1), ("wsd", 4, 256, 0), ("wsd", 8, 512, 1)],
+                         ids=lambda t: "%s-b%d-t%d-s%d" % t)
+def test_fp32_persistent_matches_tma(n, tuning):
+    """the persistent kernels (several items per CTA, short last band, up to
+    4 cells or rows per thread, x faces passed between lanes, ring of
+    stages) give the plane-per-CTA TMA result"""
+    exp = configs.shear_mini(n=n)
+    outs = []
+    for sched in (tuning, ("tma", 8, 512, 0)):
+        m = configs.build_model(exp, "fp32")
+        m.set_tuning(*sched)
+        m.integrate(3)
         outs.append(m.get_state().copy())
         m.close()
-    for o in outs[1:8]:
-        assert np.array_equal(o, outs[0])
-    # the cell kernel may contract multiply-adds differently
-    assert max_rel(outs[8], outs[0]) < 1e-6
+    assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("variant", ["tma", "group", "plane", "cell"])
+@pytest.mark.parametrize("variant", ["tma", "group", "plane", "pipe", "ws", "wsd", "cell"])
 def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
     after 200 steps of the all-axes shear case."""
