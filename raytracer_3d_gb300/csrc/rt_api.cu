@@ -184,7 +184,7 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   A.g = make_grid(h);
   for (int a = 0; a < 6; a++) {
     A.t32.inv_d[a] = h->tab32 + h->toff[a];
-    A.t32.cfl[a] = h->tab32 + h->toff[6 + a];
+    A.t32.hcfl[a] = h->tab32 + h->toff[6 + a];
     A.vel[a] = (const T*)h->vel[a];
     A.vlo[a] = (const T*)h->vlo[a];
   }
@@ -212,7 +212,7 @@ static int refresh_ucfl(rt_handle* h) {
   return RT_OK;
 }
 
-// binary32 tables 1/d and dt/d on the padded range
+// binary32 tables 1/d and dt/(2d) on the padded range
 static int upload_tab32(rt_handle* h) {
   std::vector<double> hg(h->goff[8] + padded_len(h->d, 5));
   CUDA_TRY(h, cudaMemcpy(hg.data(), h->grid, hg.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -221,7 +221,7 @@ static int upload_tab32(rt_handle* h) {
     for (long long i = 0; i < padded_len(h->d, a); i++) {
       const double dd = hg[h->goff[a] + i];
       t[h->toff[a] + i] = (float)(1.0 / dd);
-      t[h->toff[6 + a] + i] = (float)(h->p.dt / dd);
+      t[h->toff[6 + a] + i] = (float)(0.5 * h->p.dt / dd);
     }
   CUDA_TRY(h, cudaMemcpy(h->tab32, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
   return RT_OK;
@@ -951,7 +951,8 @@ int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
   if (!h) return RT_ERR_ARG;
   if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA &&
       variant != RT_VARIANT_GROUP && variant != RT_VARIANT_PIPE && variant != RT_VARIANT_WS &&
-      variant != RT_VARIANT_WSD)
+      variant != RT_VARIANT_WSD && variant != RT_VARIANT_W2 && variant != RT_VARIANT_W2D &&
+      variant != RT_VARIANT_W3)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
   if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)

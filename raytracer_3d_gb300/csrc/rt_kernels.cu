@@ -284,13 +284,13 @@ __device__ __forceinline__ double boundary_flux<float>(const StepArgs<float>& A,
     const float Eb = A.E[nb_index(d, p, a, ca, -1, c[5])];
     const float Ec = A.E[p];
     const float Ed = A.E[nb_index(d, p, a, ca, +1, c[5])];
-    return (double)flux_fp32(A.vlo[a][plane_index(d, a, c)], A.t32.cfl[a][pidx(0)], Ea, Eb, Ec, Ed);
+    return (double)flux_fp32(A.vlo[a][plane_index(d, a, c)], A.t32.hcfl[a][pidx(0)], Ea, Eb, Ec, Ed);
   }
   const float Ea = A.E[nb_index(d, p, a, ca, -1, c[5])];
   const float Eb = A.E[p];
   const float Ec = A.E[nb_index(d, p, a, ca, +1, c[5])];
   const float Ed = A.E[nb_index(d, p, a, ca, +2, c[5])];
-  return (double)flux_fp32(A.vel[a][p], A.t32.cfl[a][pidx(d.n[a])], Ea, Eb, Ec, Ed);
+  return (double)flux_fp32(A.vel[a][p], A.t32.hcfl[a][pidx(d.n[a])], Ea, Eb, Ec, Ed);
 }
 
 // boundary-flux integrals bfl_{a}{s,e}, diagnose.f90:102-277.  blockIdx.z
@@ -638,8 +638,7 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
       return launch_group_nt<T, 256>(A, S, nblk, st);
     }
   }
-  if ((tn.variant == RT_VARIANT_TMA || tn.variant == RT_VARIANT_PIPE || tn.variant == RT_VARIANT_WS ||
-       tn.variant == RT_VARIANT_WSD) &&
+  if ((tn.variant == RT_VARIANT_TMA || tn.variant >= RT_VARIANT_PIPE) &&
       tma_path_ok<T>(A.d) &&
       tma_maxc((long long)A.d.n[0] * A.d.n[1], tn.threads) <= RT_TMA_MAXC) {
     const PlaneSched S = make_sched(A.d, tn);
@@ -649,9 +648,7 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
     if (tn.threads == 1024) return launch_tma_nt<T, 1024>(A, S, nblk, st);
     return launch_tma_nt<T, 256>(A, S, nblk, st);
   }
-  if ((tn.variant == RT_VARIANT_PLANE || tn.variant == RT_VARIANT_TMA || tn.variant == RT_VARIANT_PIPE ||
-       tn.variant == RT_VARIANT_GROUP || tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) &&
-      plane_ok<T>(A.d)) {
+  if ((tn.variant != RT_VARIANT_CELL) && plane_ok<T>(A.d)) {
     const PlaneSched S = make_sched(A.d, tn);
     const long long nblk = sched_items(A.d, S);
     const size_t sm = plane_smem<T>(A.d);

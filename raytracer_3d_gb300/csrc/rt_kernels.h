@@ -60,6 +60,9 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_PIPE 4
 #define RT_VARIANT_WS 5
 #define RT_VARIANT_WSD 6
+#define RT_VARIANT_W2 7
+#define RT_VARIANT_W2D 8
+#define RT_VARIANT_W3 9
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule

@@ -1,12 +1,14 @@
 // rt_persist.cu -- launchers of the persistent binary32 step kernels:
 // the two-stage pipelined kernel (rt_step5.cuh, variant RT_VARIANT_PIPE) and
 // the warp-specialised multi-stage kernel (rt_step6.cuh, variants
-// RT_VARIANT_WS with register look-ahead and RT_VARIANT_WSD without).
+// RT_VARIANT_WS with register look-ahead and RT_VARIANT_WSD without) and
+// its 2-wide block form (rt_step7.cuh, RT_VARIANT_W2 / RT_VARIANT_W2D), and
+// the form with every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3).
 // Kept in a translation unit of their own so the library builds in parallel.
 #include <algorithm>
 
 #include "rt_kernels.h"
-#include "rt_step6.cuh"
+#include "rt_step8.cuh"
 
 namespace rt {
 
@@ -120,10 +122,99 @@ cudaError_t launch_ws_pf(const StepArgs<float>& A, const PlaneSched& S, int thre
   return launch_ws_nt<512, PF>(A, S, st);
 }
 
+// ---- 2-wide block kernel ----
+int w2_rows(const Dims& d, int nt) {
+  const int nyc = nt / (d.n[0] / 2);
+  if (nyc < 1) return 0;
+  const int R = (d.n[1] + nyc - 1) / nyc;
+  return R <= 1 ? 1 : (R <= 2 ? 2 : (R <= 4 ? 4 : 0));
+}
+bool w2_ok(const Dims& d, int threads) {
+  if (threads != 128 && threads != 256 && threads != 512) return false;
+  return d.n[0] >= 2 && d.n[0] % 2 == 0 && d.n[1] >= 2 && tma_ok<float>(d) && d.n[0] / 2 <= threads &&
+         w2_rows(d, threads) > 0 && (long long)d.n[0] * d.n[1] <= 4096 && dense_items(d) < (1LL << 31) &&
+         ws_stages(d) >= 2;
+}
+
+template <int NT, int R, int PF>
+cudaError_t launch_w2_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int ns = ws_stages(A.d);
+  const size_t sm = ws_smem(A.d, ns);
+  cudaError_t e = set_smem(step_w2_kernel<NT, R, PF>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d);
+  long long grid = 0;
+  e = persistent_grid(step_w2_kernel<NT, R, PF>, NT + 32, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_w2_kernel<NT, R, PF><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
+  return cudaGetLastError();
+}
+
+template <int NT, int PF>
+cudaError_t launch_w2_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int R = w2_rows(A.d, NT);
+  if (R == 1) return launch_w2_r<NT, 1, PF>(A, S, st);
+  if (R == 2) return launch_w2_r<NT, 2, PF>(A, S, st);
+  return launch_w2_r<NT, 4, PF>(A, S, st);
+}
+
+template <int PF>
+cudaError_t launch_w2_pf(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st) {
+  if (threads == 128) return launch_w2_nt<128, PF>(A, S, st);
+  if (threads == 256) return launch_w2_nt<256, PF>(A, S, st);
+  return launch_w2_nt<512, PF>(A, S, st);
+}
+
+// ---- all operands staged ----
+int w3_stages(const Dims& d) {
+  const long long room = (long long)ws_max_smem() - (long long)ws_head_bytes();
+  const long long per = (long long)(w3_stage_floats(d) * sizeof(float));
+  const long long ns = room > 0 ? room / per : 0;
+  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
+}
+bool w3_ok(const Dims& d, int threads) {
+  return w2_ok(d, threads) && d.n[0] % 4 == 0 && d.n[1] % 4 == 0 && w3_stages(d) >= 2;
+}
+
+template <int NT, int R>
+cudaError_t launch_w3_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int ns = w3_stages(A.d);
+  const size_t sm = w3_smem(A.d, ns);
+  cudaError_t e = set_smem(step_w3_kernel<NT, R>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d);
+  long long grid = 0;
+  e = persistent_grid(step_w3_kernel<NT, R>, NT + 32, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_w3_kernel<NT, R><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
+  return cudaGetLastError();
+}
+
+template <int NT>
+cudaError_t launch_w3_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int R = w2_rows(A.d, NT);
+  if (R == 1) return launch_w3_r<NT, 1>(A, S, st);
+  if (R == 2) return launch_w3_r<NT, 2>(A, S, st);
+  return launch_w3_r<NT, 4>(A, S, st);
+}
+
 }  // namespace
 
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
   done = false;
+  if (tn.variant == RT_VARIANT_W3 && w3_ok(A.d, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.threads == 128) return launch_w3_nt<128>(A, S, st);
+    if (tn.threads == 256) return launch_w3_nt<256>(A, S, st);
+    return launch_w3_nt<512>(A, S, st);
+  }
+  if ((tn.variant == RT_VARIANT_W2 || tn.variant == RT_VARIANT_W2D) && w2_ok(A.d, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.variant == RT_VARIANT_W2) return launch_w2_pf<1>(A, S, tn.threads, st);
+    return launch_w2_pf<0>(A, S, tn.threads, st);
+  }
   if ((tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) && ws_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);

@@ -44,30 +44,37 @@ __device__ __forceinline__ double flux_fp64u(double v, double uCFL, double Ea, d
 }
 
 // ---- binary32 precision form -------------------------------------------
-// Same flux with the limiter written without a division: for Rj != 0,
-// phi(r)*Rj with r = up/Rj equals s*max(0, min(|Rj|, 2t), min(2|Rj|, t)),
-// s = sign(Rj), t = s*up; for Rj == 0 the diffusive term vanishes exactly
-// as in the reference (it is multiplied by Rj).  cfl = dt/d(f).
-__device__ __forceinline__ float flux_fp32(float v, float cfl, float Ea, float Eb, float Ec, float Ed) {
+// Same flux, rearranged without a division.  With s = sign(Rj), t = s*up
+// and a = |Rj|, the limited slope phi(r)*Rj (r = up/Rj) is
+//   s * max(0, min(2*min(a, t), max(a, t)))
+// (= s*max(0, min(a, 2t), min(2a, t)), the superbee form, exactly: the
+// doubling is exact), and the centred part plus the first diffusive part,
+// 0.5*(v*(Ec+Eb) - |v|*Rj), is the upwind value v*E_up exactly, so
+//   F = v*E_up + |v|*(1/2 - |v|*dt/(2d)) * psi.
+// For Rj == 0 psi = 0 and the diffusive term vanishes as in the reference
+// (it is multiplied by Rj there).  hcfl = dt/(2 d(f)).
+__device__ __forceinline__ float flux_fp32(float v, float hcfl, float Ea, float Eb, float Ec, float Ed) {
   const float Rjp = Ed - Ec;
   const float Rj = Ec - Eb;
   const float Rjm = Eb - Ea;
-  const float up = v > 0.f ? Rjm : Rjp;
+  const bool pos = v > 0.f;
+  const float up = pos ? Rjm : Rjp;
+  const float Eu = pos ? Eb : Ec;
+  const bool rp = Rj >= 0.f;
   const float a = fabsf(Rj);
-  const float t = Rj >= 0.f ? up : -up;
-  const float ph = fmaxf(0.f, fmaxf(fminf(a, 2.f * t), fminf(2.f * a, t)));
-  const float psi = Rj >= 0.f ? ph : -ph;
+  const float t = rp ? up : -up;
+  const float ph = fmaxf(0.f, fminf(2.f * fminf(a, t), fmaxf(a, t)));
+  const float psi = rp ? ph : -ph;
   const float av = fabsf(v);
-  const float uCFL = av * cfl;
-  const float dif = av * (Rj - (1.f - uCFL) * psi);
-  return 0.5f * (v * (Ec + Eb) - dif);
+  const float h = av * fmaf(-hcfl, av, 0.5f);
+  return fmaf(h, psi, v * Eu);
 }
 
-// Per-axis small tables of the binary32 form: 1/d(f) and dt/d(f) on the
-// padded index range (Fortran index f at position f+1).
+// Per-axis small tables of the binary32 form: 1/d(f) and dt/(2 d(f)) on
+// the padded index range (Fortran index f at position f+1).
 struct Tab32 {
   const float* inv_d[6];
-  const float* cfl[6];
+  const float* hcfl[6];
 };
 
 template <class T>
@@ -162,8 +169,8 @@ __device__ __forceinline__ CellTerms<float> cell_terms<float>(const StepArgs<flo
     const int F = ca + 1;
     const float vr = A.vel[a][p];
     const float vl = ca > 0 ? A.vel[a][p - d.s[a]] : A.vlo[a][plane_index(d, a, c)];
-    const float fr = flux_fp32(vr, A.t32.cfl[a][pidx(F)], Em1, e0, Ep1, Ep2);
-    const float fl = flux_fp32(vl, A.t32.cfl[a][pidx(F - 1)], Em2, Em1, e0, Ep1);
+    const float fr = flux_fp32(vr, A.t32.hcfl[a][pidx(F)], Em1, e0, Ep1, Ep2);
+    const float fl = flux_fp32(vl, A.t32.hcfl[a][pidx(F - 1)], Em2, Em1, e0, Ep1);
     dE -= (fr - fl) * A.t32.inv_d[a][pidx(F)];
   }
   const float mf = e0 * A.lam[0][p];

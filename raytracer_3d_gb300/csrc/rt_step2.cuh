@@ -47,7 +47,7 @@ template <> __device__ __forceinline__ double face_flux<double>(const StepArgs<d
 template <> __device__ __forceinline__ float face_flux<float>(const StepArgs<float>& A, int a, int F,
                                                              float v, float Ea, float Eb, float Ec,
                                                              float Ed) {
-  return flux_fp32(v, A.t32.cfl[a][pidx(F)], Ea, Eb, Ec, Ed);
+  return flux_fp32(v, A.t32.hcfl[a][pidx(F)], Ea, Eb, Ec, Ed);
 }
 
 // dE -= (fr - fl) / d(F)

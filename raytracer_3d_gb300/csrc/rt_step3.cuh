@@ -111,13 +111,13 @@ __device__ __forceinline__ long long nb_plane(const Dims& d, const int c[6], int
   return p;
 }
 
-// grid constants of one face: binary32 form keeps dt/d and 1/d, binary64
+// grid constants of one face: binary32 form keeps dt/(2d) and 1/d, binary64
 // keeps d (the reference divides)
 template <class T> struct FaceK;
 template <> struct FaceK<float> {
   float cfl, inv;
   __device__ __forceinline__ void load(const StepArgs<float>& A, int a, int F, bool with_inv) {
-    cfl = A.t32.cfl[a][pidx(F)];
+    cfl = A.t32.hcfl[a][pidx(F)];
     inv = with_inv ? A.t32.inv_d[a][pidx(F)] : 0.f;
   }
 };
@@ -128,7 +128,7 @@ template <> struct FaceK<double> {
   }
 };
 // u: the cached uCFL of the face (binary64 form); the binary32 form forms
-// |v|*dt/d from its table instead
+// |v|*dt/(2d) from its table instead
 __device__ __forceinline__ float kflux(const StepArgs<float>&, const FaceK<float>& k, float v, float,
                                        float Ea, float Eb, float Ec, float Ed) {
   return flux_fp32(v, k.cfl, Ea, Eb, Ec, Ed);
@@ -219,9 +219,9 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
       desc->vloff[a] = off;
       if (d.n[a] > 1) {
         if constexpr (sizeof(T) == 4) {
-          desc->kcfl_r[a] = A.t32.cfl[a][pidx(c[a] + 1)];
+          desc->kcfl_r[a] = A.t32.hcfl[a][pidx(c[a] + 1)];
           desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
-          desc->kcfl_l[a] = A.t32.cfl[a][pidx(c[a])];
+          desc->kcfl_l[a] = A.t32.hcfl[a][pidx(c[a])];
         } else {
           desc->d_r[a] = A.g.d[a][pidx(c[a] + 1)];
           desc->d_l[a] = A.g.d[a][pidx(c[a])];

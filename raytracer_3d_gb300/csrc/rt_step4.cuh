@@ -134,9 +134,9 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
       desc->vloff[a] = off;
       if (d.n[a] > 1) {
         if constexpr (sizeof(T) == 4) {
-          desc->kcfl_r[a] = A.t32.cfl[a][pidx(c[a] + 1)];
+          desc->kcfl_r[a] = A.t32.hcfl[a][pidx(c[a] + 1)];
           desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
-          desc->kcfl_l[a] = A.t32.cfl[a][pidx(c[a])];
+          desc->kcfl_l[a] = A.t32.hcfl[a][pidx(c[a])];
         } else {
           desc->d_r[a] = A.g.d[a][pidx(c[a] + 1)];
           desc->d_l[a] = A.g.d[a][pidx(c[a])];

@@ -101,9 +101,9 @@ __device__ __forceinline__ void pipe_issue(const StepArgs<float>& A, const int c
 #pragma unroll
   for (int a = 2; a < 6; a++) {
     if (d.n[a] > 1) {
-      desc->kcfl_r[a] = A.t32.cfl[a][pidx(c[a] + 1)];
+      desc->kcfl_r[a] = A.t32.hcfl[a][pidx(c[a] + 1)];
       desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
-      desc->kcfl_l[a] = A.t32.cfl[a][pidx(c[a])];
+      desc->kcfl_l[a] = A.t32.hcfl[a][pidx(c[a])];
     }
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -197,12 +197,12 @@ __global__ void __launch_bounds__(NT, 1) step_pipe_kernel(StepArgs<float> A, Pla
           const int r = y * nx;
           const int xm = x > 0 ? x - 1 : 0, xp = x + 1 < nx ? x + 1 : nx - 1,
                     xpp = x + 2 < nx ? x + 2 : nx - 1;
-          sFx[q] = flux_fp32(cur.vx[j], A.t32.cfl[0][pidx(x + 1)], sE[r + xm], sE[q], sE[r + xp], sE[r + xpp]);
+          sFx[q] = flux_fp32(cur.vx[j], A.t32.hcfl[0][pidx(x + 1)], sE[r + xm], sE[q], sE[r + xp], sE[r + xpp]);
         }
         if (ny > 1) {
           const int ym = y > 0 ? y - 1 : 0, yp = y + 1 < ny ? y + 1 : ny - 1,
                     ypp = y + 2 < ny ? y + 2 : ny - 1;
-          sFy[q] = flux_fp32(cur.vy[j], A.t32.cfl[1][pidx(y + 1)], sE[ym * nx + x], sE[q], sE[yp * nx + x],
+          sFy[q] = flux_fp32(cur.vy[j], A.t32.hcfl[1][pidx(y + 1)], sE[ym * nx + x], sE[q], sE[yp * nx + x],
                              sE[ypp * nx + x]);
         }
       }

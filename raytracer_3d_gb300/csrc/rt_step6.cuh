@@ -124,9 +124,9 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
         D.vl[a - 2] = A.vlo[a] + off;
       }
       if (d.n[a] > 1) {
-        D.kcfl_r[a - 2] = A.t32.cfl[a][pidx(c[a] + 1)];
+        D.kcfl_r[a - 2] = A.t32.hcfl[a][pidx(c[a] + 1)];
         D.kinv_r[a - 2] = A.t32.inv_d[a][pidx(c[a] + 1)];
-        D.kcfl_l[a - 2] = A.t32.cfl[a][pidx(c[a])];
+        D.kcfl_l[a - 2] = A.t32.hcfl[a][pidx(c[a])];
       } else {
         D.kcfl_r[a - 2] = 0.f;
         D.kinv_r[a - 2] = 0.f;
@@ -233,15 +233,15 @@ __global__ void __launch_bounds__(NT + 32, (WsMinBlocks<NT, R>::value))
   for (int r = 0; r < R; r++) yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
   const int xm = x > 0 ? x - 1 : 0, xp = x + 1 < nx ? x + 1 : nx - 1, xpp = x + 2 < nx ? x + 2 : nx - 1,
             xmm = x > 1 ? x - 2 : 0;
-  const float cx = A.t32.cfl[0][pidx(x + 1)], ix = A.t32.inv_d[0][pidx(x + 1)];
-  const float cxl = A.t32.cfl[0][pidx(x)];
+  const float cx = A.t32.hcfl[0][pidx(x + 1)], ix = A.t32.inv_d[0][pidx(x + 1)];
+  const float cxl = A.t32.hcfl[0][pidx(x)];
   float cy[R], iy[R];
 #pragma unroll
   for (int r = 0; r < R; r++) {
-    cy[r] = A.t32.cfl[1][pidx(yrow[r] + 1)];
+    cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
     iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
   }
-  const float cyb = A.t32.cfl[1][pidx(y0 < ny ? y0 : ny - 1)];
+  const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
   // smem offsets of the column's rows y0-2 .. y0+R+1 (clamped)
   int ecol[R + 4];
 #pragma unroll

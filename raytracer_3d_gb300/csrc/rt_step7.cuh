@@ -1,0 +1,224 @@
+// rt_step7.cuh -- warp-specialised multi-stage step with 2-wide cell blocks
+// (binary32 form).
+//
+// Same producer, stage ring, descriptors and item order as rt_step6.cuh.
+// A consumer thread owns a block of 2 (x) by R (y) cells: columns
+// x0 = 2*(t % (nx/2)), x0+1 and rows y0 = (t / (nx/2))*R ... y0+R-1, so
+// every shared-memory and global access of the block is an 8-byte pair.
+// x faces: the thread computes the right faces of both columns; the left
+// face of x0 comes from the lane to the left by a warp shuffle (face 0 is
+// the open-boundary flux; the first lane of a warp with x0 > 0 computes it).
+// y faces: once per face inside the rows, plus the face below row y0.
+// The arithmetic per face and per cell (flux_fp32, axis order x,y,z,k,l,m,
+// divergence and update) is that of the other binary32 kernels, so results
+// are bit-identical to them.  Requires nx even.
+#pragma once
+#include "rt_step6.cuh"
+
+namespace rt {
+
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ float2 ld2_stream(const float* p) {
+  return __ldcs(reinterpret_cast<const float2*>(p));
+}
+__device__ __forceinline__ void st2_stream(float* p, float2 v) { __stcs(reinterpret_cast<float2*>(p), v); }
+
+template <int R>
+struct W2Regs {
+  float2 vx[R], vy[R], vr[4][R], vl[4][R], lam[R];
+  float xl[R];   // x0 == 0: face-0 velocity of the row; first lane with x0 > 0: velocity of face x0
+  float2 yb;     // y0 == 0: face-0 velocities of both columns; else velocities of face y0
+};
+
+template <int R>
+__device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& D, int x0, int y0,
+                                        const int yrow[R], int lane, W2Regs<R>& G) {
+  const Dims& d = A.d;
+  const int nx = d.n[0], ny = d.n[1];
+  const long long p0 = D.p0;
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int q = yrow[r] * nx + x0;
+    const long long o = p0 + q;
+    G.vx[r] = ld2_stream(A.vel[0] + o);
+    G.vy[r] = ld2_stream(A.vel[1] + o);
+#pragma unroll
+    for (int a = 2; a < 6; a++) {
+      const bool act = d.n[a] > 1;
+      G.vr[a - 2][r] = act ? ld2(A.vel[a] + o) : make_float2(0.f, 0.f);
+      G.vl[a - 2][r] = act ? ld2(D.vl[a - 2] + q) : make_float2(0.f, 0.f);
+    }
+    G.lam[r] = ld2_stream(A.lam[0] + o);
+    G.xl[r] = x0 == 0 ? D.b0x[yrow[r]] : (lane == 0 ? A.vel[0][o - 1] : 0.f);
+  }
+  G.yb = y0 == 0 ? ld2(D.b0y + x0)
+                 : (y0 < ny ? ld2(A.vel[1] + p0 + (long long)(y0 - 1) * nx + x0) : make_float2(0.f, 0.f));
+}
+
+template <int NT, int R>
+struct W2MinBlocks { static constexpr int value = 1; };
+
+template <int NT, int R, int PF>
+__global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
+    step_w2_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* empty = full + RT_WS_MAXSTAGE;
+  uint64_t* dful = empty + RT_WS_MAXSTAGE;
+  WsDesc* desc = reinterpret_cast<WsDesc*>(smem_raw + 128);
+  float* stage0 = reinterpret_cast<float*>(smem_raw + ws_head_bytes());
+  const Dims& d = A.d;
+  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ns; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NT);
+      mbar_init(&dful[s], 1);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= nitems) return;
+
+  if (threadIdx.x >= NT) {
+    if (threadIdx.x == NT) ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    return;
+  }
+
+  // ---- consumer: the thread's 2 x R block, fixed for every item ----
+  const int t = threadIdx.x, lane = t & 31;
+  const int hx = nx >> 1;
+  const int x0 = 2 * (t % hx), y0 = (t / hx) * R;
+  int yrow[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
+  // x offsets: x0-1 and x0-2 (clamped), the pair at x0+2 (absent at the right edge)
+  const int xm = x0 > 0 ? x0 - 1 : 0, xmm = x0 > 1 ? x0 - 2 : 0;
+  const bool has_right = x0 + 2 < nx;
+  const float cxa = A.t32.hcfl[0][pidx(x0 + 1)], cxb = A.t32.hcfl[0][pidx(x0 + 2)];
+  const float ixa = A.t32.inv_d[0][pidx(x0 + 1)], ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  const float cxl = A.t32.hcfl[0][pidx(x0)];
+  float cy[R], iy[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
+    iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
+  }
+  const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
+  int ecol[R + 4];   // rows y0-2 .. y0+R+1 (clamped), column pair x0
+#pragma unroll
+  for (int j = 0; j < R + 4; j++) {
+    int yy = y0 + j - 2;
+    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
+    ecol[j] = yy * nx + x0;
+  }
+  const float dt = (float)A.dt;
+
+  W2Regs<R> cur, nxt;
+  if (PF) {
+    if (!ws_wait(&dful[0], 0, A.status)) return;
+    w2_load<R>(A, desc[0], x0, y0, yrow, lane, cur);
+  }
+
+  int s = 0;
+  uint32_t par = 0;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    int sn = s + 1;
+    uint32_t parn = par;
+    if (sn == ns) { sn = 0; parn ^= 1u; }
+    if (PF) {
+      if (it + gridDim.x < nitems) {
+        if (!ws_wait(&dful[sn], parn, A.status)) return;
+        w2_load<R>(A, desc[sn], x0, y0, yrow, lane, nxt);
+      }
+    } else {
+      if (!ws_wait(&dful[s], par, A.status)) return;
+      w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur);
+    }
+    const WsDesc& D = desc[s];
+    const long long p0 = D.p0;
+    float kcr[4], kir[4], kcl[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      kcr[a] = D.kcfl_r[a];
+      kir[a] = D.kinv_r[a];
+      kcl[a] = D.kcfl_l[a];
+    }
+    if (!ws_wait(&full[s], par, A.status)) return;
+    const float* sE = stage0 + (size_t)s * RT_NPLANE * nxy;
+
+    float2 ec[R + 4];
+#pragma unroll
+    for (int j = 0; j < R + 4; j++) ec[j] = ld2(sE + ecol[j]);
+    // ---- x faces ----
+    float fxa[R], fxb[R], fxl[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int rb = yrow[r] * nx;
+      const float2 e01 = ec[r + 2];
+      const float em = sE[rb + xm];
+      const float2 e23 = has_right ? ld2(sE + rb + x0 + 2) : make_float2(e01.y, e01.y);
+      fxa[r] = flux_fp32(cur.vx[r].x, cxa, em, e01.x, e01.y, e23.x);
+      fxb[r] = flux_fp32(cur.vx[r].y, cxb, e01.x, e01.y, e23.x, e23.y);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxb[r], 1);
+    if (x0 == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++) fxl[r] = open_face0_flux<float>(cur.xl[r], ec[r + 2].x);
+    } else if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int rb = yrow[r] * nx;
+        fxl[r] = flux_fp32(cur.xl[r], cxl, sE[rb + xmm], sE[rb + x0 - 1], ec[r + 2].x, ec[r + 2].y);
+      }
+    }
+    // ---- y faces (both columns) ----
+    float2 fy[R + 1];
+    if (y0 == 0) {
+      fy[0].x = open_face0_flux<float>(cur.yb.x, ec[2].x);
+      fy[0].y = open_face0_flux<float>(cur.yb.y, ec[2].y);
+    } else {
+      fy[0].x = flux_fp32(cur.yb.x, cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
+      fy[0].y = flux_fp32(cur.yb.y, cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      fy[r + 1].x = flux_fp32(cur.vy[r].x, cy[r], ec[r + 1].x, ec[r + 2].x, ec[r + 3].x, ec[r + 4].x);
+      fy[r + 1].y = flux_fp32(cur.vy[r].y, cy[r], ec[r + 1].y, ec[r + 2].y, ec[r + 3].y, ec[r + 4].y);
+    }
+    // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 e0 = ec[r + 2];
+      const int q = yrow[r] * nx + x0;
+      float dEa = 0.f, dEb = 0.f;
+      dEa -= (fxa[r] - fxl[r]) * ixa;
+      dEb -= (fxb[r] - fxa[r]) * ixb;
+      dEa -= (fy[r + 1].x - fy[r].x) * iy[r];
+      dEb -= (fy[r + 1].y - fy[r].y) * iy[r];
+#pragma unroll
+      for (int a = 2; a < 6; a++) {
+        if (d.n[a] <= 1) continue;
+        const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
+        const float2 Em2 = ld2(sN), Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
+        const float2 vr = cur.vr[a - 2][r], vl = cur.vl[a - 2][r];
+        const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
+        const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
+        dEa -= (fra - fla) * kir[a - 2];
+        const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
+        const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+        dEb -= (frb - flb) * kir[a - 2];
+      }
+      const float mfa = e0.x * cur.lam[r].x, mfb = e0.y * cur.lam[r].y;
+      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, make_float2(e0.x + dt * (dEa - mfa), e0.y + dt * (dEb - mfb)));
+    }
+    mbar_arrive(&empty[s]);
+    if (PF) cur = nxt;
+    s = sn;
+    par = parn;
+  }
+}
+
+}  // namespace rt

@@ -1,0 +1,269 @@
+// rt_step8.cuh -- warp-specialised step with every operand staged by TMA
+// (binary32 form).
+//
+// As rt_step7.cuh (producer warp, ring of stages, 2-wide cell blocks,
+// shuffled x faces, register-chained y faces), but a stage holds everything
+// one item reads: the 17 planes of E, the 11 planes of face velocities and
+// growth rate (x and y right faces, right and left faces of z,k,l,m, the
+// combined rate) and the two face-0 rows of the plane (x faces by y, y
+// faces by x).  The consumers issue no global load at all: their operands
+// are in shared memory when the stage's mbarrier completes, so no warp
+// waits on HBM latency; the producer runs up to ns-1 items ahead.
+// Requires nx and ny multiples of 4 (16-byte rows of the face-0 copies).
+// Results are bit-identical to the other binary32 step kernels.
+#pragma once
+#include "rt_step7.cuh"
+
+namespace rt {
+
+// stage layout (floats): E planes [0,17), velocity/rate planes [17,28),
+// face-0 x row (ny), face-0 y row (nx)
+#define RT_W3_EPL 17
+#define RT_W3_NPL 28
+#define RT_W3_VX 17
+#define RT_W3_VY 18
+#define RT_W3_VR 19   // + a-2
+#define RT_W3_VL 23   // + a-2
+#define RT_W3_LAM 27
+
+__host__ __device__ __forceinline__ size_t w3_stage_floats(const Dims& d) {
+  return (size_t)RT_W3_NPL * d.n[0] * d.n[1] + d.n[1] + d.n[0];
+}
+__host__ __device__ __forceinline__ size_t w3_smem(const Dims& d, int ns) {
+  return ws_head_bytes() + (size_t)ns * w3_stage_floats(d) * sizeof(float);
+}
+
+// producer: descriptors and the bulk copies of one item per stage
+__device__ __forceinline__ void w3_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
+                                           int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
+                                           WsDesc* desc, float* stage0) {
+  const Dims& d = A.d;
+  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
+  const uint32_t pbytes = (uint32_t)(nxy * sizeof(float));
+  const size_t sfl = w3_stage_floats(d);
+  uint32_t nact = 0;
+  for (int a = 2; a < 6; a++)
+    if (d.n[a] > 1) nact++;
+  // E centre + 4 neighbours and 2 velocity planes per active axis, x/y
+  // velocities, rate, and the two face-0 rows
+  const uint32_t tx = (1 + 4 * nact + 2 * nact + 3) * pbytes + (uint32_t)((nx + ny) * sizeof(float));
+  int s = 0;
+  uint32_t rnd = 0;
+  long long issued = 0;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    if (rnd > 0 && !ws_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+    int c[6];
+    ws_decode(d, S, (unsigned)it, c);
+    const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+                         (long long)c[5] * d.s[5];
+    WsDesc& D = desc[s];
+    D.p0 = p0;
+    long long o0 = 0, o1 = 0;
+#pragma unroll
+    for (int b = 2; b < 6; b++) {
+      o0 += (long long)c[b] * d.ps[0][b];
+      o1 += (long long)c[b] * d.ps[1][b];
+    }
+    D.b0x = A.vlo[0] + o0;
+    D.b0y = A.vlo[1] + o1;
+#pragma unroll
+    for (int a = 2; a < 6; a++) {
+      if (c[a] > 0) {
+        D.vl[a - 2] = A.vel[a] + (p0 - d.s[a]);
+      } else {
+        long long off = 0;
+#pragma unroll
+        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+        D.vl[a - 2] = A.vlo[a] + off;
+      }
+      const bool act = d.n[a] > 1;
+      D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
+      D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
+      D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
+    }
+    mbar_arrive(&dful[s]);
+    float* sP = stage0 + (size_t)s * sfl;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(&full[s], tx);
+    bulk_g2s(sP, A.E + p0, pbytes, &full[s]);
+    for (int a = 2; a < 6; a++) {
+      if (d.n[a] <= 1) continue;
+      const int offs[4] = {-2, -1, 1, 2};
+      for (int j = 0; j < 4; j++)
+        bulk_g2s(sP + (size_t)(1 + 4 * (a - 2) + j) * nxy, A.E + nb_plane(d, c, a, offs[j]), pbytes, &full[s]);
+      bulk_g2s(sP + (size_t)(RT_W3_VR + a - 2) * nxy, A.vel[a] + p0, pbytes, &full[s]);
+      bulk_g2s(sP + (size_t)(RT_W3_VL + a - 2) * nxy, D.vl[a - 2], pbytes, &full[s]);
+    }
+    bulk_g2s(sP + (size_t)RT_W3_VX * nxy, A.vel[0] + p0, pbytes, &full[s]);
+    bulk_g2s(sP + (size_t)RT_W3_VY * nxy, A.vel[1] + p0, pbytes, &full[s]);
+    bulk_g2s(sP + (size_t)RT_W3_LAM * nxy, A.lam[0] + p0, pbytes, &full[s]);
+    bulk_g2s(sP + (size_t)RT_W3_NPL * nxy, D.b0x, (uint32_t)(ny * sizeof(float)), &full[s]);
+    bulk_g2s(sP + (size_t)RT_W3_NPL * nxy + ny, D.b0y, (uint32_t)(nx * sizeof(float)), &full[s]);
+    issued++;
+    if (++s == ns) { s = 0; rnd++; }
+  }
+  for (int j = 0; j < ns; j++) {
+    const long long uses = issued / ns + (j < issued % ns ? 1 : 0);
+    if (uses == 0) continue;
+    for (uint32_t w = 0; w < RT_WAIT_LIMIT; w++)
+      if (mbar_try_wait(&full[j], (uint32_t)((uses - 1) & 1))) break;
+  }
+}
+
+template <int NT, int R>
+__global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, PlaneSched S, long long nitems,
+                                                            int ns) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* empty = full + RT_WS_MAXSTAGE;
+  uint64_t* dful = empty + RT_WS_MAXSTAGE;
+  WsDesc* desc = reinterpret_cast<WsDesc*>(smem_raw + 128);
+  float* stage0 = reinterpret_cast<float*>(smem_raw + ws_head_bytes());
+  const Dims& d = A.d;
+  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
+  const size_t sfl = w3_stage_floats(d);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ns; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NT);
+      mbar_init(&dful[s], 1);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= nitems) return;
+
+  if (threadIdx.x >= NT) {
+    if (threadIdx.x == NT) w3_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    return;
+  }
+
+  // ---- consumer: the thread's 2 x R block, fixed for every item ----
+  const int t = threadIdx.x, lane = t & 31;
+  const int hx = nx >> 1;
+  const int x0 = 2 * (t % hx), y0 = (t / hx) * R;
+  int yrow[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
+  const int xm = x0 > 0 ? x0 - 1 : 0, xmm = x0 > 1 ? x0 - 2 : 0;
+  const bool has_right = x0 + 2 < nx;
+  const float cxa = A.t32.hcfl[0][pidx(x0 + 1)], cxb = A.t32.hcfl[0][pidx(x0 + 2)];
+  const float ixa = A.t32.inv_d[0][pidx(x0 + 1)], ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  const float cxl = A.t32.hcfl[0][pidx(x0)];
+  float cy[R], iy[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
+    iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
+  }
+  const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
+  int ecol[R + 4];
+#pragma unroll
+  for (int j = 0; j < R + 4; j++) {
+    int yy = y0 + j - 2;
+    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
+    ecol[j] = yy * nx + x0;
+  }
+  // smem offset of the y velocities below the block (row y0-1) or of the
+  // face-0 y row (y0 == 0)
+  const int yb_off = y0 == 0 ? RT_W3_NPL * nxy + ny + x0
+                              : RT_W3_VY * nxy + ((y0 - 1 < ny - 1 ? y0 - 1 : ny - 1)) * nx + x0;
+  const float dt = (float)A.dt;
+
+  int s = 0;
+  uint32_t par = 0;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    if (!ws_wait(&dful[s], par, A.status)) return;
+    const WsDesc& D = desc[s];
+    const long long p0 = D.p0;
+    float kcr[4], kir[4], kcl[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      kcr[a] = D.kcfl_r[a];
+      kir[a] = D.kinv_r[a];
+      kcl[a] = D.kcfl_l[a];
+    }
+    if (!ws_wait(&full[s], par, A.status)) return;
+    const float* sE = stage0 + (size_t)s * sfl;
+
+    float2 ec[R + 4];
+#pragma unroll
+    for (int j = 0; j < R + 4; j++) ec[j] = ld2(sE + ecol[j]);
+    // ---- x faces ----
+    float fxa[R], fxb[R], fxl[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int rb = yrow[r] * nx;
+      const float2 e01 = ec[r + 2];
+      const float em = sE[rb + xm];
+      const float2 e23 = has_right ? ld2(sE + rb + x0 + 2) : make_float2(e01.y, e01.y);
+      const float2 vx = ld2(sE + RT_W3_VX * nxy + rb + x0);
+      fxa[r] = flux_fp32(vx.x, cxa, em, e01.x, e01.y, e23.x);
+      fxb[r] = flux_fp32(vx.y, cxb, e01.x, e01.y, e23.x, e23.y);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxb[r], 1);
+    if (x0 == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++)
+        fxl[r] = open_face0_flux<float>(sE[RT_W3_NPL * nxy + yrow[r]], ec[r + 2].x);
+    } else if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int rb = yrow[r] * nx;
+        fxl[r] = flux_fp32(sE[RT_W3_VX * nxy + rb + x0 - 1], cxl, sE[rb + xmm], sE[rb + x0 - 1], ec[r + 2].x,
+                           ec[r + 2].y);
+      }
+    }
+    // ---- y faces (both columns) ----
+    float2 fy[R + 1];
+    {
+      const float2 vb = ld2(sE + yb_off);
+      if (y0 == 0) {
+        fy[0].x = open_face0_flux<float>(vb.x, ec[2].x);
+        fy[0].y = open_face0_flux<float>(vb.y, ec[2].y);
+      } else {
+        fy[0].x = flux_fp32(vb.x, cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
+        fy[0].y = flux_fp32(vb.y, cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 vy = ld2(sE + RT_W3_VY * nxy + yrow[r] * nx + x0);
+      fy[r + 1].x = flux_fp32(vy.x, cy[r], ec[r + 1].x, ec[r + 2].x, ec[r + 3].x, ec[r + 4].x);
+      fy[r + 1].y = flux_fp32(vy.y, cy[r], ec[r + 1].y, ec[r + 2].y, ec[r + 3].y, ec[r + 4].y);
+    }
+    // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 e0 = ec[r + 2];
+      const int q = yrow[r] * nx + x0;
+      float dEa = 0.f, dEb = 0.f;
+      dEa -= (fxa[r] - fxl[r]) * ixa;
+      dEb -= (fxb[r] - fxa[r]) * ixb;
+      dEa -= (fy[r + 1].x - fy[r].x) * iy[r];
+      dEb -= (fy[r + 1].y - fy[r].y) * iy[r];
+#pragma unroll
+      for (int a = 2; a < 6; a++) {
+        if (d.n[a] <= 1) continue;
+        const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
+        const float2 Em2 = ld2(sN), Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
+        const float2 vr = ld2(sE + (RT_W3_VR + a - 2) * nxy + q), vl = ld2(sE + (RT_W3_VL + a - 2) * nxy + q);
+        const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
+        const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
+        dEa -= (fra - fla) * kir[a - 2];
+        const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
+        const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+        dEb -= (frb - flb) * kir[a - 2];
+      }
+      const float2 lam = ld2(sE + RT_W3_LAM * nxy + q);
+      const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
+      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, make_float2(e0.x + dt * (dEa - mfa), e0.y + dt * (dEb - mfb)));
+    }
+    mbar_arrive(&empty[s]);
+    if (++s == ns) { s = 0; par ^= 1u; }
+  }
+}
+
+}  // namespace rt
