@@ -63,6 +63,9 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_W2 7
 #define RT_VARIANT_W2D 8
 #define RT_VARIANT_W3 9
+#define RT_VARIANT_W4 10
+#define RT_VARIANT_W5 11
+#define RT_VARIANT_W5H 12
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule

@@ -3,12 +3,15 @@
 // the warp-specialised multi-stage kernel (rt_step6.cuh, variants
 // RT_VARIANT_WS with register look-ahead and RT_VARIANT_WSD without) and
 // its 2-wide block form (rt_step7.cuh, RT_VARIANT_W2 / RT_VARIANT_W2D), and
-// the form with every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3).
+// the form with every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3),
+// the form with the producer folded into warp 0 (rt_step9.cuh,
+// RT_VARIANT_W4), and the row-chunk form with consumer groups (rt_step10.cuh,
+// RT_VARIANT_W5 with 256-thread groups, RT_VARIANT_W5H with 128).
 // Kept in a translation unit of their own so the library builds in parallel.
 #include <algorithm>
 
 #include "rt_kernels.h"
-#include "rt_step8.cuh"
+#include "rt_step10.cuh"
 
 namespace rt {
 
@@ -198,10 +201,108 @@ cudaError_t launch_w3_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStre
   return launch_w3_r<NT, 4>(A, S, st);
 }
 
+// ---- producer in warp 0 ----
+template <int NT, int R>
+cudaError_t launch_w4_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int ns = ws_stages(A.d);
+  const size_t sm = ws_smem(A.d, ns);
+  cudaError_t e = set_smem(step_w4_kernel<NT, R>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d);
+  long long grid = 0;
+  e = persistent_grid(step_w4_kernel<NT, R>, NT, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_w4_kernel<NT, R><<<(unsigned)grid, NT, sm, st>>>(A, S, nitems, ns);
+  return cudaGetLastError();
+}
+
+template <int NT>
+cudaError_t launch_w4_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const int R = w2_rows(A.d, NT);
+  if (R == 1) return launch_w4_r<NT, 1>(A, S, st);
+  if (R == 2) return launch_w4_r<NT, 2>(A, S, st);
+  return launch_w4_r<NT, 4>(A, S, st);
+}
+
+// ---- row chunks, consumer groups ----
+// rows per thread R and rows per chunk hr for groups of gt threads: hr is a
+// multiple of 4 (16-byte rows of the face-0 copy), at least 4
+struct W5Shape {
+  int R = 0, hr = 0, nyc = 0, ns = 0;
+};
+W5Shape w5_shape(const Dims& d, int gt, int ng) {
+  W5Shape w;
+  const int nx = d.n[0], ny = d.n[1];
+  if (nx < 4 || nx % 4 || ny < 4 || ny % 4 || nx / 2 > gt) return w;
+  const int chunks = gt / (nx / 2);
+  for (int R = 1; R <= 2; R++) {
+    int hr = chunks * R / 4 * 4;
+    if (hr > ny) hr = ny;
+    if (hr >= 4) {
+      w.R = R;
+      w.hr = hr;
+      break;
+    }
+  }
+  if (!w.R) return w;
+  w.nyc = (ny + w.hr - 1) / w.hr;
+  W5Layout L{nx, w.hr};
+  const long long room = (long long)ws_max_smem() - (long long)w5_head_bytes();
+  const long long per = (long long)L.floats() * (long long)sizeof(float);
+  w.ns = (int)std::min<long long>(room > 0 ? room / per : 0, RT_WS_MAXSTAGE);
+  if (w.ns < ng + 1) w.R = 0;
+  return w;
+}
+bool w5_ok(const Dims& d, int gt, int threads) {
+  if (threads % gt || threads / gt < 1 || threads / gt > 4) return false;
+  const W5Shape w = w5_shape(d, gt, threads / gt);
+  return w.R > 0 && d.n[0] >= 4 && tma_ok<float>(d) && dense_items(d) * w.nyc < (1LL << 31);
+}
+
+template <int GT, int NG, int R>
+cudaError_t launch_w5_r(const StepArgs<float>& A, const PlaneSched& S, const W5Shape& w, cudaStream_t st) {
+  const size_t sm = w5_smem(A.d, w.hr, w.ns);
+  cudaError_t e = set_smem(step_w5_kernel<GT, NG, R>, sm);
+  if (e != cudaSuccess) return e;
+  const long long nitems = dense_items(A.d) * w.nyc;
+  long long grid = 0;
+  e = persistent_grid(step_w5_kernel<GT, NG, R>, GT * NG + 32, sm, nitems, grid);
+  if (e != cudaSuccess) return e;
+  step_w5_kernel<GT, NG, R><<<(unsigned)grid, GT * NG + 32, sm, st>>>(A, S, nitems, w.nyc, w.hr, w.ns);
+  return cudaGetLastError();
+}
+
+template <int GT, int NG>
+cudaError_t launch_w5_ng(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
+  const W5Shape w = w5_shape(A.d, GT, NG);
+  if (w.R == 1) return launch_w5_r<GT, NG, 1>(A, S, w, st);
+  return launch_w5_r<GT, NG, 2>(A, S, w, st);
+}
+
 }  // namespace
 
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
   done = false;
+  if (tn.variant == RT_VARIANT_W5 && w5_ok(A.d, 256, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.threads == 256) return launch_w5_ng<256, 1>(A, S, st);
+    return launch_w5_ng<256, 2>(A, S, st);
+  }
+  if (tn.variant == RT_VARIANT_W5H && w5_ok(A.d, 128, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.threads == 128) return launch_w5_ng<128, 1>(A, S, st);
+    if (tn.threads == 256) return launch_w5_ng<128, 2>(A, S, st);
+    return launch_w5_ng<128, 4>(A, S, st);
+  }
+  if (tn.variant == RT_VARIANT_W4 && w2_ok(A.d, tn.threads)) {
+    done = true;
+    const PlaneSched S = make_sched(A.d, tn);
+    if (tn.threads == 128) return launch_w4_nt<128>(A, S, st);
+    if (tn.threads == 256) return launch_w4_nt<256>(A, S, st);
+    return launch_w4_nt<512>(A, S, st);
+  }
   if (tn.variant == RT_VARIANT_W3 && w3_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);

@@ -4,7 +4,7 @@
 // rt_step5.cuh, walked by persistent CTAs (CTA b takes items b, b+G, ...).
 // Each CTA has NT consumer threads and one producer warp:
 //
-//   producer (one thread): decodes the next items, writes their descriptors
+//   producer (one warp): decodes the next items, writes their descriptors
 //     (plane offset, left-face velocity bases, face-0 bases, grid constants)
 //     into shared memory and issues the 17 bulk copies of E of each item into
 //     a ring of `ns` stages (2..4, as many as fit).  Stage s is refilled only
@@ -59,6 +59,16 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, int* sta
   return false;
 }
 
+// bounded wait of a whole warp: lane 0 polls, the result is broadcast, and
+// __syncwarp orders the other lanes' later accesses after lane 0's acquire
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* status) {
+  bool ok = true;
+  if ((threadIdx.x & 31) == 0) ok = ws_wait(bar, parity, status);
+  ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+  __syncwarp();
+  return ok;
+}
+
 // item -> (z,k,l,m) in band order without holes, 32-bit arithmetic (the
 // launcher checks that the item count is below 2^31)
 __device__ __forceinline__ void ws_decode(const Dims& d, const PlaneSched& S, unsigned item, int c[6]) {
@@ -83,11 +93,14 @@ __device__ __forceinline__ void ws_decode(const Dims& d, const PlaneSched& S, un
   c[5] = S.sweep ? (int)outer : banded;
 }
 
-// producer: one thread of the last warp
+// producer: the 32 lanes of the last warp.  All lanes decode the item;
+// lane 0 publishes the descriptor and arms the stage; lane j < 17 issues the
+// bulk copy of plane j (0 = centre, 1 + 4(a-2) + i = neighbour i of axis a).
 __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
                                            int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
                                            WsDesc* desc, float* stage0) {
   const Dims& d = A.d;
+  const int lane = threadIdx.x & 31;
   const int nxy = d.n[0] * d.n[1];
   const uint32_t pbytes = (uint32_t)(nxy * sizeof(float));
   uint32_t nplanes = 1;
@@ -98,53 +111,53 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
   long long issued = 0;
   for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
     // stage s is free once every consumer thread released its previous item
-    if (rnd > 0 && !ws_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+    if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
     int c[6];
     ws_decode(d, S, (unsigned)it, c);
     const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                          (long long)c[5] * d.s[5];
-    WsDesc& D = desc[s];
-    D.p0 = p0;
-    long long o0 = 0, o1 = 0;
+    if (lane == 0) {
+      WsDesc& D = desc[s];
+      D.p0 = p0;
+      long long o0 = 0, o1 = 0;
 #pragma unroll
-    for (int b = 2; b < 6; b++) {
-      o0 += (long long)c[b] * d.ps[0][b];
-      o1 += (long long)c[b] * d.ps[1][b];
-    }
-    D.b0x = A.vlo[0] + o0;
-    D.b0y = A.vlo[1] + o1;
-#pragma unroll
-    for (int a = 2; a < 6; a++) {
-      if (c[a] > 0) {
-        D.vl[a - 2] = A.vel[a] + (p0 - d.s[a]);
-      } else {
-        long long off = 0;
-#pragma unroll
-        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-        D.vl[a - 2] = A.vlo[a] + off;
+      for (int b = 2; b < 6; b++) {
+        o0 += (long long)c[b] * d.ps[0][b];
+        o1 += (long long)c[b] * d.ps[1][b];
       }
-      if (d.n[a] > 1) {
-        D.kcfl_r[a - 2] = A.t32.hcfl[a][pidx(c[a] + 1)];
-        D.kinv_r[a - 2] = A.t32.inv_d[a][pidx(c[a] + 1)];
-        D.kcfl_l[a - 2] = A.t32.hcfl[a][pidx(c[a])];
-      } else {
-        D.kcfl_r[a - 2] = 0.f;
-        D.kinv_r[a - 2] = 0.f;
-        D.kcfl_l[a - 2] = 0.f;
+      D.b0x = A.vlo[0] + o0;
+      D.b0y = A.vlo[1] + o1;
+#pragma unroll
+      for (int a = 2; a < 6; a++) {
+        if (c[a] > 0) {
+          D.vl[a - 2] = A.vel[a] + (p0 - d.s[a]);
+        } else {
+          long long off = 0;
+#pragma unroll
+          for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+          D.vl[a - 2] = A.vlo[a] + off;
+        }
+        const bool act = d.n[a] > 1;
+        D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
+        D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
+        D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
       }
+      mbar_arrive(&dful[s]);   // release: the descriptor is visible to waiters
+      mbar_arrive_expect_tx(&full[s], nplanes * pbytes);
     }
-    mbar_arrive(&dful[s]);   // release: the descriptor is visible to waiters
-    float* sP = stage0 + (size_t)s * RT_NPLANE * nxy;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive_expect_tx(&full[s], nplanes * pbytes);
-    bulk_g2s(sP, A.E + p0, pbytes, &full[s]);
-    int slot = 1;
-    for (int a = 2; a < 6; a++) {
-      if (d.n[a] <= 1) { slot += 4; continue; }
-      const int offs[4] = {-2, -1, 1, 2};
-      for (int j = 0; j < 4; j++)
-        bulk_g2s(sP + (size_t)(slot + j) * nxy, A.E + nb_plane(d, c, a, offs[j]), pbytes, &full[s]);
-      slot += 4;
+    __syncwarp();
+    if (lane < RT_NPLANE) {
+      bool go = true;
+      long long off = p0;
+      if (lane > 0) {
+        const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
+        go = d.n[a] > 1;
+        if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
+      }
+      if (go) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bulk_g2s(stage0 + (size_t)s * RT_NPLANE * nxy + (size_t)lane * nxy, A.E + off, pbytes, &full[s]);
+      }
     }
     issued++;
     if (++s == ns) { s = 0; rnd++; }
@@ -221,7 +234,7 @@ __global__ void __launch_bounds__(NT + 32, (WsMinBlocks<NT, R>::value))
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    if (threadIdx.x == NT) ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
     return;
   }
 

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    if (threadIdx.x == NT) ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
     return;
   }
 

@@ -33,11 +33,15 @@ __host__ __device__ __forceinline__ size_t w3_smem(const Dims& d, int ns) {
   return ws_head_bytes() + (size_t)ns * w3_stage_floats(d) * sizeof(float);
 }
 
-// producer: descriptors and the bulk copies of one item per stage
+// producer: the 32 lanes of the last warp; lane 0 publishes the descriptor
+// and arms the stage, lane j issues copy j: 0..16 the E planes (as
+// rt_step6.cuh), 17..20 right and 21..24 left face velocities of z..m,
+// 25 x and 26 y velocities, 27 the rate, 28 and 29 the face-0 rows
 __device__ __forceinline__ void w3_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
                                            int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
                                            WsDesc* desc, float* stage0) {
   const Dims& d = A.d;
+  const int lane = threadIdx.x & 31;
   const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
   const uint32_t pbytes = (uint32_t)(nxy * sizeof(float));
   const size_t sfl = w3_stage_floats(d);
@@ -51,54 +55,71 @@ __device__ __forceinline__ void w3_produce(const StepArgs<float>& A, const Plane
   uint32_t rnd = 0;
   long long issued = 0;
   for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-    if (rnd > 0 && !ws_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+    if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
     int c[6];
     ws_decode(d, S, (unsigned)it, c);
     const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                          (long long)c[5] * d.s[5];
-    WsDesc& D = desc[s];
-    D.p0 = p0;
-    long long o0 = 0, o1 = 0;
+    if (lane == 0) {
+      WsDesc& D = desc[s];
+      D.p0 = p0;
 #pragma unroll
-    for (int b = 2; b < 6; b++) {
-      o0 += (long long)c[b] * d.ps[0][b];
-      o1 += (long long)c[b] * d.ps[1][b];
-    }
-    D.b0x = A.vlo[0] + o0;
-    D.b0y = A.vlo[1] + o1;
-#pragma unroll
-    for (int a = 2; a < 6; a++) {
-      if (c[a] > 0) {
-        D.vl[a - 2] = A.vel[a] + (p0 - d.s[a]);
-      } else {
-        long long off = 0;
-#pragma unroll
-        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-        D.vl[a - 2] = A.vlo[a] + off;
+      for (int a = 2; a < 6; a++) {
+        const bool act = d.n[a] > 1;
+        D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
+        D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
+        D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
       }
-      const bool act = d.n[a] > 1;
-      D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
-      D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
-      D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
+      mbar_arrive(&dful[s]);
+      mbar_arrive_expect_tx(&full[s], tx);
     }
-    mbar_arrive(&dful[s]);
+    __syncwarp();
     float* sP = stage0 + (size_t)s * sfl;
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive_expect_tx(&full[s], tx);
-    bulk_g2s(sP, A.E + p0, pbytes, &full[s]);
-    for (int a = 2; a < 6; a++) {
-      if (d.n[a] <= 1) continue;
-      const int offs[4] = {-2, -1, 1, 2};
-      for (int j = 0; j < 4; j++)
-        bulk_g2s(sP + (size_t)(1 + 4 * (a - 2) + j) * nxy, A.E + nb_plane(d, c, a, offs[j]), pbytes, &full[s]);
-      bulk_g2s(sP + (size_t)(RT_W3_VR + a - 2) * nxy, A.vel[a] + p0, pbytes, &full[s]);
-      bulk_g2s(sP + (size_t)(RT_W3_VL + a - 2) * nxy, D.vl[a - 2], pbytes, &full[s]);
+    const float* src = nullptr;
+    float* dst = nullptr;
+    uint32_t bytes = pbytes;
+    if (lane < RT_NPLANE) {
+      long long off = p0;
+      bool go = true;
+      if (lane > 0) {
+        const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
+        go = d.n[a] > 1;
+        if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
+      }
+      if (go) { src = A.E + off; dst = sP + (size_t)lane * nxy; }
+    } else if (lane < 25) {
+      const bool right = lane < 21;
+      const int a = 2 + (right ? lane - 17 : lane - 21);
+      if (d.n[a] > 1) {
+        if (right) {
+          src = A.vel[a] + p0;
+        } else if (c[a] > 0) {
+          src = A.vel[a] + (p0 - d.s[a]);
+        } else {
+          long long off = 0;
+#pragma unroll
+          for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+          src = A.vlo[a] + off;
+        }
+        dst = sP + (size_t)((right ? RT_W3_VR : RT_W3_VL) + a - 2) * nxy;
+      }
+    } else if (lane < 28) {
+      const int which = lane - 25;   // x velocity, y velocity, rate
+      src = (which == 0 ? A.vel[0] : (which == 1 ? A.vel[1] : A.lam[0])) + p0;
+      dst = sP + (size_t)(which == 0 ? RT_W3_VX : (which == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
+    } else if (lane < 30) {
+      long long off = 0;
+      const int a = lane - 28;   // face-0 x row (by y), face-0 y row (by x)
+#pragma unroll
+      for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+      src = A.vlo[a] + off;
+      dst = sP + (size_t)RT_W3_NPL * nxy + (a == 0 ? 0 : ny);
+      bytes = (uint32_t)((a == 0 ? ny : nx) * sizeof(float));
     }
-    bulk_g2s(sP + (size_t)RT_W3_VX * nxy, A.vel[0] + p0, pbytes, &full[s]);
-    bulk_g2s(sP + (size_t)RT_W3_VY * nxy, A.vel[1] + p0, pbytes, &full[s]);
-    bulk_g2s(sP + (size_t)RT_W3_LAM * nxy, A.lam[0] + p0, pbytes, &full[s]);
-    bulk_g2s(sP + (size_t)RT_W3_NPL * nxy, D.b0x, (uint32_t)(ny * sizeof(float)), &full[s]);
-    bulk_g2s(sP + (size_t)RT_W3_NPL * nxy + ny, D.b0y, (uint32_t)(nx * sizeof(float)), &full[s]);
+    if (src) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_g2s(dst, src, bytes, &full[s]);
+    }
     issued++;
     if (++s == ns) { s = 0; rnd++; }
   }
@@ -135,7 +156,7 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    if (threadIdx.x == NT) w3_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    w3_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
     return;
   }
 
