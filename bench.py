@@ -261,7 +261,9 @@ def bench_batched(steps, warmup, members=48, seed=2024):
     cells = b.cells
     out = {"value": cells * steps / secs, "unit": UNIT, "members": members, "cells_per_step": cells,
            "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": b.launch_count() - l0,
-           "graph_steps": b.tuning[3], "tuning": {"band": best[0], "threads": best[1], "sweep": best[2]},
+           "graph_steps": b.tuning[3],
+           "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
+                      "persistent_members": b.persistent_members()},
            "roofline": roofline("fp32", cells, secs / steps), "clocks": cs.summary(),
            "setup_s": round(setup_s, 2)}
     b.close()

@@ -205,6 +205,14 @@ const char* rt_batch_last_error(const rt_batch* b);
 /* band, CTA size (128/256/512/1024), sweep order (0/1) and steps per captured
  * graph (even); chosen by the autotuner (raytracer_3d_gb300.autotune) */
 int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps);
+/* binary32 members whose x-y planes fill a CTA of `threads` consumer
+ * threads (128/256/512; x and y extents multiples of 4) are stepped by the
+ * batched warp-specialised kernel with every operand staged by bulk copies,
+ * the others by the z-group / plane kernels; 0 puts every member in the
+ * latter class.  Default 256.  No effect on results. */
+int rt_batch_set_persistent(rt_batch* b, int threads);
+/* number of members in the warp-specialised class (negative: error) */
+int rt_batch_persistent_members(rt_batch* b);
 /* advance every member by nsteps (asynchronous on the batch stream) */
 int rt_batch_integrate(rt_batch* b, int nsteps);
 int rt_batch_sync(rt_batch* b);

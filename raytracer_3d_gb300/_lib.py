@@ -72,6 +72,8 @@ SIGNATURES = {
     "rt_batch_destroy": (ctypes.c_int, [_P]),
     "rt_batch_last_error": (ctypes.c_char_p, [_P]),
     "rt_batch_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "rt_batch_set_persistent": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_batch_persistent_members": (ctypes.c_int, [_P]),
     "rt_batch_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_batch_sync": (ctypes.c_int, [_P]),
     "rt_batch_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),

@@ -26,6 +26,7 @@ class Batch:
         for m in self.models:
             m._state_on_device = True
         self.tuning = (8, 256, 0, 16)
+        self.persistent = 256
 
     def _check(self, rc, what):
         if rc != 0:
@@ -34,6 +35,17 @@ class Batch:
     def set_tuning(self, band=8, threads=256, sweep=0, graph_steps=16):
         self._check(self._lib.rt_batch_set_tuning(self._b, band, threads, sweep, graph_steps), "rt_batch_set_tuning")
         self.tuning = (band, threads, sweep, graph_steps)
+
+    def set_persistent(self, threads=256):
+        """consumer threads of the warp-specialised class (0: off)"""
+        self._check(self._lib.rt_batch_set_persistent(self._b, int(threads)), "rt_batch_set_persistent")
+        self.persistent = int(threads)
+
+    def persistent_members(self):
+        n = self._lib.rt_batch_persistent_members(self._b)
+        if n < 0:
+            self._check(n, "rt_batch_persistent_members")
+        return int(n)
 
     def integrate(self, nsteps):
         self._check(self._lib.rt_batch_integrate(self._b, int(nsteps)), "rt_batch_integrate")

@@ -259,6 +259,15 @@ struct rt_batch {
   long long cells = 0;
   cudaEvent_t ev = nullptr;
   std::string err;
+  // members stepped by the batched fully staged kernel (binary32 form, planes
+  // that fill a CTA of pthreads consumer threads); the others use the arrays
+  // above (nq members)
+  int pthreads = 256;           // 0: every member in the other class
+  int np = 0, nq = 0;
+  void* d_pmem[2] = {nullptr, nullptr};
+  long long* d_pfirst = nullptr;
+  int pR = 0, pns = 0, pgrid = 0;
+  long long pstage = 0;         // floats per stage
 };
 
 static int bfail(rt_batch* b, int code, const char* fmt, ...) {
@@ -284,28 +293,102 @@ static void batch_free_graphs(rt_batch* b) {
     if (b->gexec[k]) { cudaGraphExecDestroy(b->gexec[k]); b->gexec[k] = nullptr; }
 }
 
+// kernel launches per batch step
+static int batch_kernels(const rt_batch* b) { return (b->np > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0); }
+
+// one step of every member, starting from the arrays of parity `par`
 template <class T>
-static cudaError_t batch_launch(rt_batch* b, const void* mem) {
-  const int n = (int)b->mem.size();
+static cudaError_t batch_launch(rt_batch* b, int par) {
+  cudaError_t e = cudaSuccess;
+  if (b->np)
+    e = launch_batch_w3(b->d_pmem[par], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage, b->pgrid, b->st);
+  if (e != cudaSuccess || !b->nq) return e;
+  const void* mem = b->d_mem[par];
+  const int n = b->nq;
   if (b->group) return launch_batch_group<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
   if (b->tma)
     return launch_batch_tma<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->max_nxy, b->st);
   return launch_batch<T>(mem, b->d_first, n, b->smem, b->tune.threads, b->grid, b->st);
 }
 
+// binary32 members whose planes fill the fully staged kernel's CTA form the
+// persistent class; its arrays, stage size and grid
+template <class T>
+static int batch_build_persistent(rt_batch* b, std::vector<int>& rest) {
+  const int n = (int)b->mem.size();
+  rest.clear();
+  b->np = 0;
+  std::vector<int> pm;
+  if (sizeof(T) == 4 && b->pthreads > 0) {
+    int Rc = 0;
+    for (int j = 0; j < n; j++) Rc = std::max(Rc, batch_w3_rows(b->mem[j]->d, b->pthreads, 0));
+    for (int j = 0; j < n; j++)
+      if (Rc > 0 && batch_w3_rows(b->mem[j]->d, b->pthreads, Rc) > 0) pm.push_back(j);
+      else rest.push_back(j);
+    long long stage = 0;
+    for (int j : pm) stage = std::max(stage, batch_w3_stage_floats(b->mem[j]->d));
+    const int ns = pm.empty() ? 0 : batch_w3_stages(stage);
+    if (ns < 2) {   // no member, or the largest plane leaves no room for two stages
+      for (int j : pm) rest.push_back(j);
+      std::sort(rest.begin(), rest.end());
+      pm.clear();
+    } else {
+      b->pR = Rc;
+      b->pns = ns;
+      b->pstage = stage;
+    }
+  } else {
+    for (int j = 0; j < n; j++) rest.push_back(j);
+  }
+  if (pm.empty()) return RT_OK;
+  std::vector<BatchMember<float>> arr[2];
+  std::vector<long long> first(pm.size() + 1, 0);
+  for (size_t i = 0; i < pm.size(); i++) {
+    rt_handle* h = b->mem[pm[i]];
+    for (int par = 0; par < 2; par++) {
+      BatchMember<float> bm;
+      bm.A = make_step_args<float>(h, par == 0 ? h->cur : 1 - h->cur);
+      bm.S = make_sched(h->d, b->tune);
+      arr[par].push_back(bm);
+    }
+    first[i + 1] = first[i] + (long long)h->d.n[2] * h->d.n[3] * h->d.n[4] * h->d.n[5];
+    b->cur0[pm[i]] = h->cur;
+  }
+  for (int par = 0; par < 2; par++) {
+    if (!b->d_pmem[par]) BCUDA_TRY(b, cudaMalloc(&b->d_pmem[par], (size_t)n * sizeof(BatchMember<float>)));
+    BCUDA_TRY(b, cudaMemcpy(b->d_pmem[par], arr[par].data(), pm.size() * sizeof(BatchMember<float>),
+                            cudaMemcpyHostToDevice));
+  }
+  if (!b->d_pfirst) BCUDA_TRY(b, cudaMalloc(&b->d_pfirst, (size_t)(n + 1) * sizeof(long long)));
+  BCUDA_TRY(b, cudaMemcpy(b->d_pfirst, first.data(), first.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  const int per_sm = batch_w3_blocks_per_sm(b->pthreads, b->pR, batch_w3_smem(b->pns, b->pstage));
+  if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batched staged kernel does not fit on an SM");
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  b->pgrid = (int)std::min<long long>(first.back(), (long long)per_sm * nsm);
+  b->np = (int)pm.size();
+  return RT_OK;
+}
+
 template <class T>
 static int batch_build(rt_batch* b) {
-  const int n = (int)b->mem.size();
+  std::vector<int> qm;   // members of the plane / group / TMA class
+  int rc = batch_build_persistent<T>(b, qm);
+  if (rc) return rc;
+  const int n = (int)qm.size();
+  b->nq = n;
   std::vector<BatchMember<T>> arr[2];
   std::vector<long long> first(n + 1, 0);
   size_t smem = 0;
   bool tma = true, group = true;
   b->max_nxy = 0;
   std::vector<int> gz(n, 1);
-  for (int j = 0; j < n; j++) {
+  for (int i = 0; i < n; i++) {
+    const int j = qm[i];
     tma = tma && tma_path_ok<T>(b->mem[j]->d);
-    gz[j] = group_size<T>(b->mem[j]->d, b->tune);
-    group = group && gz[j] > 0;
+    gz[i] = group_size<T>(b->mem[j]->d, b->tune);
+    group = group && gz[i] > 0;
     b->max_nxy = std::max(b->max_nxy, (long long)b->mem[j]->d.n[0] * b->mem[j]->d.n[1]);
   }
   // z-group items are preferred: they keep the CTA busy on small planes
@@ -314,38 +397,41 @@ static int batch_build(rt_batch* b) {
   if ((b->max_nxy + b->tune.threads - 1) / b->tune.threads > RT_TMA_MAXC) tma = false;
   // the plain-load batch kernel has no 1024-thread form
   if (!tma && !group && b->tune.threads > 512) b->tune.threads = 512;
-  for (int j = 0; j < n; j++) {
-    rt_handle* h = b->mem[j];
+  for (int i = 0; i < n; i++) {
+    rt_handle* h = b->mem[qm[i]];
     StepTuning tn = b->tune;
     for (int par = 0; par < 2; par++) {
       BatchMember<T> bm;
       bm.A = make_step_args<T>(h, par == 0 ? h->cur : 1 - h->cur);
-      bm.S = make_sched(h->d, tn, group ? gz[j] : 1);
+      bm.S = make_sched(h->d, tn, group ? gz[i] : 1);
       arr[par].push_back(bm);
     }
-    first[j + 1] = first[j] + sched_items(h->d, arr[0].back().S);
-    smem = std::max(smem, group ? group_path_smem<T>(h->d, gz[j])
+    first[i + 1] = first[i] + sched_items(h->d, arr[0].back().S);
+    smem = std::max(smem, group ? group_path_smem<T>(h->d, gz[i])
                                 : (tma ? tma_path_smem<T>(h->d) : plane_smem<T>(h->d)));
-    b->cur0[j] = h->cur;
+    b->cur0[qm[i]] = h->cur;
   }
-  for (int par = 0; par < 2; par++) {
-    if (!b->d_mem[par]) BCUDA_TRY(b, cudaMalloc(&b->d_mem[par], (size_t)n * sizeof(BatchMember<T>)));
-    BCUDA_TRY(b, cudaMemcpy(b->d_mem[par], arr[par].data(), (size_t)n * sizeof(BatchMember<T>),
+  if (n > 0) {
+    const int nall = (int)b->mem.size();
+    for (int par = 0; par < 2; par++) {
+      if (!b->d_mem[par]) BCUDA_TRY(b, cudaMalloc(&b->d_mem[par], (size_t)nall * sizeof(BatchMember<T>)));
+      BCUDA_TRY(b, cudaMemcpy(b->d_mem[par], arr[par].data(), (size_t)n * sizeof(BatchMember<T>),
+                              cudaMemcpyHostToDevice));
+    }
+    if (!b->d_first) BCUDA_TRY(b, cudaMalloc(&b->d_first, (size_t)(nall + 1) * sizeof(long long)));
+    BCUDA_TRY(b, cudaMemcpy(b->d_first, first.data(), (size_t)(n + 1) * sizeof(long long),
                             cudaMemcpyHostToDevice));
+    b->smem = smem;
+    b->tma = tma;
+    b->group = group;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = batch_blocks_per_sm<T>(b->tune.threads, smem, tma, group);
+    if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batch kernel does not fit on an SM");
+    const long long items = first[n];
+    b->grid = (int)std::min<long long>(items, (long long)per_sm * nsm);
   }
-  if (!b->d_first) BCUDA_TRY(b, cudaMalloc(&b->d_first, (size_t)(n + 1) * sizeof(long long)));
-  BCUDA_TRY(b, cudaMemcpy(b->d_first, first.data(), (size_t)(n + 1) * sizeof(long long),
-                          cudaMemcpyHostToDevice));
-  b->smem = smem;
-  b->tma = tma;
-  b->group = group;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int per_sm = batch_blocks_per_sm<T>(b->tune.threads, smem, tma, group);
-  if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batch kernel does not fit on an SM");
-  const long long items = first[n];
-  b->grid = (int)std::min<long long>(items, (long long)per_sm * nsm);
   b->parity = 0;
   // capture graph_steps launches starting at each parity
   batch_free_graphs(b);
@@ -354,7 +440,7 @@ static int batch_build(rt_batch* b) {
     BCUDA_TRY(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int t = 0; t < b->graph_steps && e == cudaSuccess; t++)
-      e = batch_launch<T>(b, b->d_mem[(start + t) & 1]);
+      e = batch_launch<T>(b, (start + t) & 1);
     cudaError_t e2 = cudaStreamEndCapture(b->st, &g);
     if (e != cudaSuccess || e2 != cudaSuccess)
       return bfail(b, RT_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
@@ -383,13 +469,13 @@ static int batch_run(rt_batch* b, int nsteps) {
   int left = nsteps;
   while (left >= b->graph_steps) {
     BCUDA_TRY(b, cudaGraphLaunch(b->gexec[b->parity], b->st));
-    b->launches += b->graph_steps;
+    b->launches += (long long)b->graph_steps * batch_kernels(b);
     left -= b->graph_steps;  // graph_steps is even: parity unchanged
   }
   while (left > 0) {
-    cudaError_t e = batch_launch<T>(b, b->d_mem[b->parity]);
+    cudaError_t e = batch_launch<T>(b, b->parity);
     if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
-    b->launches += 1;
+    b->launches += batch_kernels(b);
     b->parity ^= 1;
     left -= 1;
   }
@@ -444,8 +530,12 @@ int rt_batch_destroy(rt_batch* b) {
   if (!b) return RT_OK;
   if (b->st) cudaStreamSynchronize(b->st);
   batch_free_graphs(b);
-  for (int k = 0; k < 2; k++) cudaFree(b->d_mem[k]);
+  for (int k = 0; k < 2; k++) {
+    cudaFree(b->d_mem[k]);
+    cudaFree(b->d_pmem[k]);
+  }
   cudaFree(b->d_first);
+  cudaFree(b->d_pfirst);
   if (b->ev) cudaEventDestroy(b->ev);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -470,6 +560,25 @@ int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph
   return RT_OK;
 }
 
+int rt_batch_set_persistent(rt_batch* b, int threads) {
+  if (!b) return RT_ERR_ARG;
+  if (threads != 0 && threads != 128 && threads != 256 && threads != 512)
+    return bfail(b, RT_ERR_ARG, "rt_batch_set_persistent: threads must be 0, 128, 256 or 512");
+  cudaStreamSynchronize(b->st);
+  b->pthreads = threads;
+  b->dirty = true;
+  return RT_OK;
+}
+
+int rt_batch_persistent_members(rt_batch* b) {
+  if (!b) return RT_ERR_ARG;
+  if (b->dirty) {
+    const int rc = b->fp64 ? batch_build<double>(b) : batch_build<float>(b);
+    if (rc) return rc;
+  }
+  return b->np;
+}
+
 int rt_batch_integrate(rt_batch* b, int nsteps) {
   if (!b) return RT_ERR_ARG;
   if (nsteps < 0) return bfail(b, RT_ERR_ARG, "rt_batch_integrate: nsteps < 0");
@@ -489,9 +598,9 @@ int rt_batch_dry(rt_batch* b, int nsteps) {
     if (rc) return rc;
   }
   for (int t = 0; t < nsteps; t++) {
-    cudaError_t e = b->fp64 ? batch_launch<double>(b, b->d_mem[b->parity]) : batch_launch<float>(b, b->d_mem[b->parity]);
+    cudaError_t e = b->fp64 ? batch_launch<double>(b, b->parity) : batch_launch<float>(b, b->parity);
     if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
-    b->launches += 1;
+    b->launches += batch_kernels(b);
   }
   BCUDA_TRY(b, cudaEventRecord(b->ev, b->st));
   for (int j = 0; j < n; j++) {

@@ -105,6 +105,16 @@ cudaError_t launch_batch_tma(const void* members, const long long* first, int nm
 size_t batch_member_bytes(int precision_fp64);
 template <class T>
 cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t st);
+// batched form of the fully staged persistent kernel (rt_persist.cu):
+// rows per consumer thread for a member plane (R_class > 0: the class's
+// rows), 0 when the member does not fill at least half of the CTA
+int batch_w3_rows(const Dims& d, int threads, int R_class);
+long long batch_w3_stage_floats(const Dims& d);
+int batch_w3_stages(long long stage_floats);
+size_t batch_w3_smem(int ns, long long stage_floats);
+int batch_w3_blocks_per_sm(int threads, int R, size_t smem);
+cudaError_t launch_batch_w3(const void* members, const long long* first, int nmem, int threads, int R, int ns,
+                            long long stage_floats, int grid, cudaStream_t st);
 // persistent binary32 kernels (rt_persist.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);

@@ -279,7 +279,78 @@ cudaError_t launch_w5_ng(const StepArgs<float>& A, const PlaneSched& S, cudaStre
   return launch_w5_r<GT, NG, 2>(A, S, w, st);
 }
 
+template <int NT, int R>
+cudaError_t launch_bw3_r(const void* members, const long long* first, int nmem, int ns, long long stage_floats,
+                         int grid, cudaStream_t st) {
+  const size_t sm = ws_head_bytes() + (size_t)ns * stage_floats * sizeof(float);
+  cudaError_t e = set_smem(batch_w3_kernel<NT, R>, sm);
+  if (e != cudaSuccess) return e;
+  batch_w3_kernel<NT, R><<<(unsigned)grid, NT + 32, sm, st>>>(
+      static_cast<const BatchMember<float>*>(members), first, nmem, ns, stage_floats);
+  return cudaGetLastError();
+}
+
+template <int NT>
+cudaError_t launch_bw3_nt(const void* members, const long long* first, int nmem, int R, int ns,
+                          long long stage_floats, int grid, cudaStream_t st) {
+  if (R == 1) return launch_bw3_r<NT, 1>(members, first, nmem, ns, stage_floats, grid, st);
+  if (R == 2) return launch_bw3_r<NT, 2>(members, first, nmem, ns, stage_floats, grid, st);
+  return launch_bw3_r<NT, 4>(members, first, nmem, ns, stage_floats, grid, st);
+}
+
+template <int NT>
+int bw3_per_sm_nt(int R, size_t smem) {
+  int per_sm = 0;
+  cudaError_t e;
+  if (R == 1) {
+    set_smem(batch_w3_kernel<NT, 1>, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_w3_kernel<NT, 1>, NT + 32, smem);
+  } else if (R == 2) {
+    set_smem(batch_w3_kernel<NT, 2>, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_w3_kernel<NT, 2>, NT + 32, smem);
+  } else {
+    set_smem(batch_w3_kernel<NT, 4>, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_w3_kernel<NT, 4>, NT + 32, smem);
+  }
+  return e == cudaSuccess ? per_sm : 0;
+}
+
 }  // namespace
+
+// ---- batched form of the fully staged kernel ----
+int batch_w3_rows(const Dims& d, int threads, int R_class) {
+  if (threads != 128 && threads != 256 && threads != 512) return 0;
+  const int nx = d.n[0], ny = d.n[1];
+  if (nx < 4 || nx % 4 || ny < 4 || ny % 4 || nx / 2 > threads || !tma_ok<float>(d)) return 0;
+  if (dense_items(d) >= (1LL << 31)) return 0;
+  const int R = R_class > 0 ? R_class : w2_rows(d, threads);
+  if (R <= 0) return 0;
+  const int hx = nx / 2, chunks = threads / hx;
+  if ((long long)chunks * R < ny) return 0;
+  // at least half of the consumer threads own cells of the plane
+  const long long busy = (long long)hx * ((ny + R - 1) / R);
+  return 2 * busy >= threads ? R : 0;
+}
+long long batch_w3_stage_floats(const Dims& d) { return (long long)w3_stage_floats(d); }
+int batch_w3_stages(long long stage_floats) {
+  const long long room = (long long)ws_max_smem() - (long long)ws_head_bytes();
+  const long long ns = room > 0 ? room / (stage_floats * (long long)sizeof(float)) : 0;
+  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
+}
+size_t batch_w3_smem(int ns, long long stage_floats) {
+  return ws_head_bytes() + (size_t)ns * stage_floats * sizeof(float);
+}
+int batch_w3_blocks_per_sm(int threads, int R, size_t smem) {
+  if (threads == 128) return bw3_per_sm_nt<128>(R, smem);
+  if (threads == 256) return bw3_per_sm_nt<256>(R, smem);
+  return bw3_per_sm_nt<512>(R, smem);
+}
+cudaError_t launch_batch_w3(const void* members, const long long* first, int nmem, int threads, int R, int ns,
+                            long long stage_floats, int grid, cudaStream_t st) {
+  if (threads == 128) return launch_bw3_nt<128>(members, first, nmem, R, ns, stage_floats, grid, st);
+  if (threads == 256) return launch_bw3_nt<256>(members, first, nmem, R, ns, stage_floats, grid, st);
+  return launch_bw3_nt<512>(members, first, nmem, R, ns, stage_floats, grid, st);
+}
 
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
   done = false;

@@ -37,6 +37,7 @@ struct WsDesc {
   const float* b0x;        // face-0 x velocities of the plane (index y)
   const float* b0y;        // face-0 y velocities of the plane (index x)
   float kcfl_r[4], kinv_r[4], kcfl_l[4];
+  int member;              // batched form: index of the member the item belongs to
 };
 
 __host__ __device__ constexpr size_t ws_desc_bytes() { return (sizeof(WsDesc) + 15) / 16 * 16; }

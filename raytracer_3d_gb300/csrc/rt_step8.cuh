@@ -33,101 +33,235 @@ __host__ __device__ __forceinline__ size_t w3_smem(const Dims& d, int ns) {
   return ws_head_bytes() + (size_t)ns * w3_stage_floats(d) * sizeof(float);
 }
 
-// producer: the 32 lanes of the last warp; lane 0 publishes the descriptor
-// and arms the stage, lane j issues copy j: 0..16 the E planes (as
-// rt_step6.cuh), 17..20 right and 21..24 left face velocities of z..m,
-// 25 x and 26 y velocities, 27 the rate, 28 and 29 the face-0 rows
-__device__ __forceinline__ void w3_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
-                                           int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
-                                           WsDesc* desc, float* stage0) {
+// One item into stage s, by the 32 lanes of a warp: all lanes decode it,
+// lane 0 publishes the descriptor and arms the stage, lane j issues copy j:
+// 0..16 the E planes (as rt_step6.cuh), 17..20 right and 21..24 left face
+// velocities of z..m, 25 x and 26 y velocities, 27 the rate, 28 and 29 the
+// face-0 rows.  `li` is the item's index within its field, `member` is
+// recorded in the descriptor for the batched form.
+__device__ __forceinline__ void w3_issue(const StepArgs<float>& A, const PlaneSched& S, long long li, int member,
+                                         float* sP, WsDesc* D, uint64_t* fullb, uint64_t* dfulb) {
   const Dims& d = A.d;
   const int lane = threadIdx.x & 31;
   const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
   const uint32_t pbytes = (uint32_t)(nxy * sizeof(float));
-  const size_t sfl = w3_stage_floats(d);
-  uint32_t nact = 0;
-  for (int a = 2; a < 6; a++)
-    if (d.n[a] > 1) nact++;
-  // E centre + 4 neighbours and 2 velocity planes per active axis, x/y
-  // velocities, rate, and the two face-0 rows
-  const uint32_t tx = (1 + 4 * nact + 2 * nact + 3) * pbytes + (uint32_t)((nx + ny) * sizeof(float));
-  int s = 0;
-  uint32_t rnd = 0;
-  long long issued = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-    if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
-    int c[6];
-    ws_decode(d, S, (unsigned)it, c);
-    const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
-                         (long long)c[5] * d.s[5];
-    if (lane == 0) {
-      WsDesc& D = desc[s];
-      D.p0 = p0;
+  int c[6];
+  ws_decode(d, S, (unsigned)li, c);
+  const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+                       (long long)c[5] * d.s[5];
+  if (lane == 0) {
+    uint32_t nact = 0;
+    D->p0 = p0;
+    D->member = member;
 #pragma unroll
-      for (int a = 2; a < 6; a++) {
-        const bool act = d.n[a] > 1;
-        D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
-        D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
-        D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
-      }
-      mbar_arrive(&dful[s]);
-      mbar_arrive_expect_tx(&full[s], tx);
+    for (int a = 2; a < 6; a++) {
+      const bool act = d.n[a] > 1;
+      D->kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
+      D->kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
+      D->kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
+      if (act) nact++;
     }
-    __syncwarp();
-    float* sP = stage0 + (size_t)s * sfl;
-    const float* src = nullptr;
-    float* dst = nullptr;
-    uint32_t bytes = pbytes;
-    if (lane < RT_NPLANE) {
-      long long off = p0;
-      bool go = true;
-      if (lane > 0) {
-        const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
-        go = d.n[a] > 1;
-        if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
-      }
-      if (go) { src = A.E + off; dst = sP + (size_t)lane * nxy; }
-    } else if (lane < 25) {
-      const bool right = lane < 21;
-      const int a = 2 + (right ? lane - 17 : lane - 21);
-      if (d.n[a] > 1) {
-        if (right) {
-          src = A.vel[a] + p0;
-        } else if (c[a] > 0) {
-          src = A.vel[a] + (p0 - d.s[a]);
-        } else {
-          long long off = 0;
-#pragma unroll
-          for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-          src = A.vlo[a] + off;
-        }
-        dst = sP + (size_t)((right ? RT_W3_VR : RT_W3_VL) + a - 2) * nxy;
-      }
-    } else if (lane < 28) {
-      const int which = lane - 25;   // x velocity, y velocity, rate
-      src = (which == 0 ? A.vel[0] : (which == 1 ? A.vel[1] : A.lam[0])) + p0;
-      dst = sP + (size_t)(which == 0 ? RT_W3_VX : (which == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
-    } else if (lane < 30) {
-      long long off = 0;
-      const int a = lane - 28;   // face-0 x row (by y), face-0 y row (by x)
-#pragma unroll
-      for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-      src = A.vlo[a] + off;
-      dst = sP + (size_t)RT_W3_NPL * nxy + (a == 0 ? 0 : ny);
-      bytes = (uint32_t)((a == 0 ? ny : nx) * sizeof(float));
-    }
-    if (src) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bulk_g2s(dst, src, bytes, &full[s]);
-    }
-    issued++;
-    if (++s == ns) { s = 0; rnd++; }
+    mbar_arrive(dfulb);
+    // E centre + 4 neighbours and 2 velocity planes per active axis, x/y
+    // velocities, rate, and the two face-0 rows
+    mbar_arrive_expect_tx(fullb, (1 + 6 * nact + 3) * pbytes + (uint32_t)((nx + ny) * sizeof(float)));
   }
+  __syncwarp();
+  const float* src = nullptr;
+  float* dst = nullptr;
+  uint32_t bytes = pbytes;
+  if (lane < RT_NPLANE) {
+    long long off = p0;
+    bool go = true;
+    if (lane > 0) {
+      const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
+      go = d.n[a] > 1;
+      if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
+    }
+    if (go) { src = A.E + off; dst = sP + (size_t)lane * nxy; }
+  } else if (lane < 25) {
+    const bool right = lane < 21;
+    const int a = 2 + (right ? lane - 17 : lane - 21);
+    if (d.n[a] > 1) {
+      if (right) {
+        src = A.vel[a] + p0;
+      } else if (c[a] > 0) {
+        src = A.vel[a] + (p0 - d.s[a]);
+      } else {
+        long long off = 0;
+#pragma unroll
+        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+        src = A.vlo[a] + off;
+      }
+      dst = sP + (size_t)((right ? RT_W3_VR : RT_W3_VL) + a - 2) * nxy;
+    }
+  } else if (lane < 28) {
+    const int which = lane - 25;   // x velocity, y velocity, rate
+    src = (which == 0 ? A.vel[0] : (which == 1 ? A.vel[1] : A.lam[0])) + p0;
+    dst = sP + (size_t)(which == 0 ? RT_W3_VX : (which == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
+  } else if (lane < 30) {
+    long long off = 0;
+    const int a = lane - 28;   // face-0 x row (by y), face-0 y row (by x)
+#pragma unroll
+    for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+    src = A.vlo[a] + off;
+    dst = sP + (size_t)RT_W3_NPL * nxy + (a == 0 ? 0 : ny);
+    bytes = (uint32_t)((a == 0 ? ny : nx) * sizeof(float));
+  }
+  if (src) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bulk_g2s(dst, src, bytes, fullb);
+  }
+}
+
+// producer warp after its last item: copies still in flight (only after a
+// timeout) land before the CTA can leave (bounded waits)
+__device__ __forceinline__ void ws_drain(uint64_t* full, int ns, long long issued) {
   for (int j = 0; j < ns; j++) {
     const long long uses = issued / ns + (j < issued % ns ? 1 : 0);
     if (uses == 0) continue;
     for (uint32_t w = 0; w < RT_WAIT_LIMIT; w++)
       if (mbar_try_wait(&full[j], (uint32_t)((uses - 1) & 1))) break;
+  }
+}
+
+// a consumer thread's 2 x R block of an nx x ny plane and the constants it
+// needs, fixed for every item of one field
+template <int R>
+struct W3Geom {
+  int nx, ny, nxy, x0, y0, xm, xmm, yb_off;
+  bool has_right;
+  int yrow[R], ecol[R + 4];
+  float cxa, cxb, ixa, ixb, cxl, cyb, dt;
+  float cy[R], iy[R];
+};
+
+template <int R>
+__device__ __forceinline__ void w3_geom(const StepArgs<float>& A, int t, W3Geom<R>& g) {
+  const int nx = A.d.n[0], ny = A.d.n[1];
+  g.nx = nx;
+  g.ny = ny;
+  g.nxy = nx * ny;
+  const int hx = nx >> 1;
+  g.x0 = 2 * (t % hx);
+  g.y0 = (t / hx) * R;
+  const int x0 = g.x0, y0 = g.y0;
+#pragma unroll
+  for (int r = 0; r < R; r++) g.yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
+  g.xm = x0 > 0 ? x0 - 1 : 0;
+  g.xmm = x0 > 1 ? x0 - 2 : 0;
+  g.has_right = x0 + 2 < nx;
+  g.cxa = A.t32.hcfl[0][pidx(x0 + 1)];
+  g.cxb = A.t32.hcfl[0][pidx(x0 + 2)];
+  g.ixa = A.t32.inv_d[0][pidx(x0 + 1)];
+  g.ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  g.cxl = A.t32.hcfl[0][pidx(x0)];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    g.cy[r] = A.t32.hcfl[1][pidx(g.yrow[r] + 1)];
+    g.iy[r] = A.t32.inv_d[1][pidx(g.yrow[r] + 1)];
+  }
+  g.cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
+#pragma unroll
+  for (int j = 0; j < R + 4; j++) {
+    int yy = y0 + j - 2;
+    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
+    g.ecol[j] = yy * nx + x0;
+  }
+  // smem offset of the y velocities below the block (row y0-1) or of the
+  // face-0 y row (y0 == 0)
+  g.yb_off = y0 == 0 ? RT_W3_NPL * g.nxy + ny + x0
+                     : RT_W3_VY * g.nxy + ((y0 - 1 < ny - 1 ? y0 - 1 : ny - 1)) * nx + x0;
+  g.dt = (float)A.dt;
+}
+
+// one item of one consumer thread from a filled stage
+template <int R>
+__device__ __forceinline__ void w3_item(const StepArgs<float>& A, const W3Geom<R>& g, const WsDesc& D,
+                                        const float* sE, int lane) {
+  const Dims& d = A.d;
+  const int nx = g.nx, ny = g.ny, nxy = g.nxy, x0 = g.x0, y0 = g.y0;
+  const long long p0 = D.p0;
+  float kcr[4], kir[4], kcl[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    kcr[a] = D.kcfl_r[a];
+    kir[a] = D.kinv_r[a];
+    kcl[a] = D.kcfl_l[a];
+  }
+  float2 ec[R + 4];
+#pragma unroll
+  for (int j = 0; j < R + 4; j++) ec[j] = ld2(sE + g.ecol[j]);
+  // ---- x faces ----
+  float fxa[R], fxb[R], fxl[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int rb = g.yrow[r] * nx;
+    const float2 e01 = ec[r + 2];
+    const float em = sE[rb + g.xm];
+    const float2 e23 = g.has_right ? ld2(sE + rb + x0 + 2) : make_float2(e01.y, e01.y);
+    const float2 vx = ld2(sE + RT_W3_VX * nxy + rb + x0);
+    fxa[r] = flux_fp32(vx.x, g.cxa, em, e01.x, e01.y, e23.x);
+    fxb[r] = flux_fp32(vx.y, g.cxb, e01.x, e01.y, e23.x, e23.y);
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxb[r], 1);
+  if (x0 == 0) {
+#pragma unroll
+    for (int r = 0; r < R; r++) fxl[r] = open_face0_flux<float>(sE[RT_W3_NPL * nxy + g.yrow[r]], ec[r + 2].x);
+  } else if (lane == 0) {
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int rb = g.yrow[r] * nx;
+      fxl[r] = flux_fp32(sE[RT_W3_VX * nxy + rb + x0 - 1], g.cxl, sE[rb + g.xmm], sE[rb + x0 - 1], ec[r + 2].x,
+                         ec[r + 2].y);
+    }
+  }
+  // ---- y faces (both columns) ----
+  float2 fy[R + 1];
+  {
+    const float2 vb = ld2(sE + g.yb_off);
+    if (y0 == 0) {
+      fy[0].x = open_face0_flux<float>(vb.x, ec[2].x);
+      fy[0].y = open_face0_flux<float>(vb.y, ec[2].y);
+    } else {
+      fy[0].x = flux_fp32(vb.x, g.cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
+      fy[0].y = flux_fp32(vb.y, g.cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const float2 vy = ld2(sE + RT_W3_VY * nxy + g.yrow[r] * nx + x0);
+    fy[r + 1].x = flux_fp32(vy.x, g.cy[r], ec[r + 1].x, ec[r + 2].x, ec[r + 3].x, ec[r + 4].x);
+    fy[r + 1].y = flux_fp32(vy.y, g.cy[r], ec[r + 1].y, ec[r + 2].y, ec[r + 3].y, ec[r + 4].y);
+  }
+  // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const float2 e0 = ec[r + 2];
+    const int q = g.yrow[r] * nx + x0;
+    float dEa = 0.f, dEb = 0.f;
+    dEa -= (fxa[r] - fxl[r]) * g.ixa;
+    dEb -= (fxb[r] - fxa[r]) * g.ixb;
+    dEa -= (fy[r + 1].x - fy[r].x) * g.iy[r];
+    dEb -= (fy[r + 1].y - fy[r].y) * g.iy[r];
+#pragma unroll
+    for (int a = 2; a < 6; a++) {
+      if (d.n[a] <= 1) continue;
+      const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
+      const float2 Em2 = ld2(sN), Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
+      const float2 vr = ld2(sE + (RT_W3_VR + a - 2) * nxy + q), vl = ld2(sE + (RT_W3_VL + a - 2) * nxy + q);
+      const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
+      const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
+      dEa -= (fra - fla) * kir[a - 2];
+      const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
+      const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+      dEb -= (frb - flb) * kir[a - 2];
+    }
+    const float2 lam = ld2(sE + RT_W3_LAM * nxy + q);
+    const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
+    if (y0 + r < ny)
+      st2_stream(A.Enew + p0 + q, make_float2(e0.x + g.dt * (dEa - mfa), e0.y + g.dt * (dEb - mfb)));
   }
 }
 
@@ -140,9 +274,7 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
   uint64_t* dful = empty + RT_WS_MAXSTAGE;
   WsDesc* desc = reinterpret_cast<WsDesc*>(smem_raw + 128);
   float* stage0 = reinterpret_cast<float*>(smem_raw + ws_head_bytes());
-  const Dims& d = A.d;
-  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
-  const size_t sfl = w3_stage_floats(d);
+  const size_t sfl = w3_stage_floats(A.d);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < ns; s++) {
@@ -156,132 +288,94 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    w3_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    // ---- producer warp ----
+    int s = 0;
+    uint32_t rnd = 0;
+    long long issued = 0;
+    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+      w3_issue(A, S, it, 0, stage0 + (size_t)s * sfl, &desc[s], &full[s], &dful[s]);
+      issued++;
+      if (++s == ns) { s = 0; rnd++; }
+    }
+    ws_drain(full, ns, issued);
     return;
   }
 
-  // ---- consumer: the thread's 2 x R block, fixed for every item ----
-  const int t = threadIdx.x, lane = t & 31;
-  const int hx = nx >> 1;
-  const int x0 = 2 * (t % hx), y0 = (t / hx) * R;
-  int yrow[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
-  const int xm = x0 > 0 ? x0 - 1 : 0, xmm = x0 > 1 ? x0 - 2 : 0;
-  const bool has_right = x0 + 2 < nx;
-  const float cxa = A.t32.hcfl[0][pidx(x0 + 1)], cxb = A.t32.hcfl[0][pidx(x0 + 2)];
-  const float ixa = A.t32.inv_d[0][pidx(x0 + 1)], ixb = A.t32.inv_d[0][pidx(x0 + 2)];
-  const float cxl = A.t32.hcfl[0][pidx(x0)];
-  float cy[R], iy[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
-    iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
-  }
-  const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
-  int ecol[R + 4];
-#pragma unroll
-  for (int j = 0; j < R + 4; j++) {
-    int yy = y0 + j - 2;
-    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
-    ecol[j] = yy * nx + x0;
-  }
-  // smem offset of the y velocities below the block (row y0-1) or of the
-  // face-0 y row (y0 == 0)
-  const int yb_off = y0 == 0 ? RT_W3_NPL * nxy + ny + x0
-                              : RT_W3_VY * nxy + ((y0 - 1 < ny - 1 ? y0 - 1 : ny - 1)) * nx + x0;
-  const float dt = (float)A.dt;
-
+  // ---- consumers ----
+  const int lane = threadIdx.x & 31;
+  W3Geom<R> g;
+  w3_geom<R>(A, threadIdx.x, g);
   int s = 0;
   uint32_t par = 0;
   for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
     if (!ws_wait(&dful[s], par, A.status)) return;
-    const WsDesc& D = desc[s];
-    const long long p0 = D.p0;
-    float kcr[4], kir[4], kcl[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      kcr[a] = D.kcfl_r[a];
-      kir[a] = D.kinv_r[a];
-      kcl[a] = D.kcfl_l[a];
-    }
     if (!ws_wait(&full[s], par, A.status)) return;
-    const float* sE = stage0 + (size_t)s * sfl;
+    w3_item<R>(A, g, desc[s], stage0 + (size_t)s * sfl, lane);
+    mbar_arrive(&empty[s]);
+    if (++s == ns) { s = 0; par ^= 1u; }
+  }
+}
 
-    float2 ec[R + 4];
-#pragma unroll
-    for (int j = 0; j < R + 4; j++) ec[j] = ld2(sE + ecol[j]);
-    // ---- x faces ----
-    float fxa[R], fxb[R], fxl[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const int rb = yrow[r] * nx;
-      const float2 e01 = ec[r + 2];
-      const float em = sE[rb + xm];
-      const float2 e23 = has_right ? ld2(sE + rb + x0 + 2) : make_float2(e01.y, e01.y);
-      const float2 vx = ld2(sE + RT_W3_VX * nxy + rb + x0);
-      fxa[r] = flux_fp32(vx.x, cxa, em, e01.x, e01.y, e23.x);
-      fxb[r] = flux_fp32(vx.y, cxb, e01.x, e01.y, e23.x, e23.y);
+// Batched form: the members' items one after the other (member j owns
+// items [first[j], first[j+1]) of its own band order), walked by persistent
+// CTAs; stages are sized for the largest member plane (stage_floats).  The
+// consumers recompute their block geometry when the member changes.
+template <int NT, int R>
+__global__ void __launch_bounds__(NT + 32, 1)
+    batch_w3_kernel(const BatchMember<float>* __restrict__ mem, const long long* __restrict__ first, int nmem,
+                    int ns, long long stage_floats) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* empty = full + RT_WS_MAXSTAGE;
+  uint64_t* dful = empty + RT_WS_MAXSTAGE;
+  WsDesc* desc = reinterpret_cast<WsDesc*>(smem_raw + 128);
+  float* stage0 = reinterpret_cast<float*>(smem_raw + ws_head_bytes());
+  const long long nitems = first[nmem];
+  int* status = mem[0].A.status;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ns; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NT);
+      mbar_init(&dful[s], 1);
     }
-#pragma unroll
-    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxb[r], 1);
-    if (x0 == 0) {
-#pragma unroll
-      for (int r = 0; r < R; r++)
-        fxl[r] = open_face0_flux<float>(sE[RT_W3_NPL * nxy + yrow[r]], ec[r + 2].x);
-    } else if (lane == 0) {
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        const int rb = yrow[r] * nx;
-        fxl[r] = flux_fp32(sE[RT_W3_VX * nxy + rb + x0 - 1], cxl, sE[rb + xmm], sE[rb + x0 - 1], ec[r + 2].x,
-                           ec[r + 2].y);
-      }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= nitems) return;
+
+  if (threadIdx.x >= NT) {
+    int s = 0, j = 0;
+    uint32_t rnd = 0;
+    long long issued = 0;
+    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
+      while (it >= first[j + 1]) j++;
+      w3_issue(mem[j].A, mem[j].S, it - first[j], j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s],
+               &dful[s]);
+      issued++;
+      if (++s == ns) { s = 0; rnd++; }
     }
-    // ---- y faces (both columns) ----
-    float2 fy[R + 1];
-    {
-      const float2 vb = ld2(sE + yb_off);
-      if (y0 == 0) {
-        fy[0].x = open_face0_flux<float>(vb.x, ec[2].x);
-        fy[0].y = open_face0_flux<float>(vb.y, ec[2].y);
-      } else {
-        fy[0].x = flux_fp32(vb.x, cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
-        fy[0].y = flux_fp32(vb.y, cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
-      }
+    ws_drain(full, ns, issued);
+    return;
+  }
+
+  const int lane = threadIdx.x & 31;
+  W3Geom<R> g;
+  int jc = -1;
+  int s = 0;
+  uint32_t par = 0;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    if (!ws_wait(&dful[s], par, status)) return;
+    const int j = desc[s].member;
+    const StepArgs<float>& A = mem[j].A;
+    if (j != jc) {
+      w3_geom<R>(A, threadIdx.x, g);
+      jc = j;
     }
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const float2 vy = ld2(sE + RT_W3_VY * nxy + yrow[r] * nx + x0);
-      fy[r + 1].x = flux_fp32(vy.x, cy[r], ec[r + 1].x, ec[r + 2].x, ec[r + 3].x, ec[r + 4].x);
-      fy[r + 1].y = flux_fp32(vy.y, cy[r], ec[r + 1].y, ec[r + 2].y, ec[r + 3].y, ec[r + 4].y);
-    }
-    // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const float2 e0 = ec[r + 2];
-      const int q = yrow[r] * nx + x0;
-      float dEa = 0.f, dEb = 0.f;
-      dEa -= (fxa[r] - fxl[r]) * ixa;
-      dEb -= (fxb[r] - fxa[r]) * ixb;
-      dEa -= (fy[r + 1].x - fy[r].x) * iy[r];
-      dEb -= (fy[r + 1].y - fy[r].y) * iy[r];
-#pragma unroll
-      for (int a = 2; a < 6; a++) {
-        if (d.n[a] <= 1) continue;
-        const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
-        const float2 Em2 = ld2(sN), Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
-        const float2 vr = ld2(sE + (RT_W3_VR + a - 2) * nxy + q), vl = ld2(sE + (RT_W3_VL + a - 2) * nxy + q);
-        const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
-        const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
-        dEa -= (fra - fla) * kir[a - 2];
-        const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
-        const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
-        dEb -= (frb - flb) * kir[a - 2];
-      }
-      const float2 lam = ld2(sE + RT_W3_LAM * nxy + q);
-      const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
-      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, make_float2(e0.x + dt * (dEa - mfa), e0.y + dt * (dEb - mfb)));
-    }
+    if (!ws_wait(&full[s], par, status)) return;
+    w3_item<R>(A, g, desc[s], stage0 + (size_t)s * stage_floats, lane);
     mbar_arrive(&empty[s]);
     if (++s == ns) { s = 0; par ^= 1u; }
   }

@@ -68,3 +68,39 @@ def test_member_can_leave_and_step_alone():
     b2.close()
     for m in models:
         m.close()
+
+
+@pytest.mark.parametrize("persistent", [256, 512, 128, 0])
+def test_mixed_classes_equal_members_alone(persistent):
+    """members whose planes fill the warp-specialised CTA take that kernel,
+    the others the group / plane kernels, in one captured step; every
+    member gets its result alone"""
+    from raytracer_3d_gb300.batch import Batch
+    rng = np.random.default_rng(23)
+    exps = [configs.ensemble_member(rng, steps=5, spatial=(8, 16, 24, 32), spectral=(4, 6)) for _ in range(7)]
+    exps.append(configs.ensemble_member(np.random.default_rng(3), steps=5, spatial=(32,), spectral=(4,)))
+    alone = []
+    for e in exps:
+        m = configs.build_model(e, "fp32")
+        m.integrate(e.steps)
+        alone.append(m.get_state().copy())
+        m.close()
+    models = [configs.build_model(e, "fp32") for e in exps]
+    b = Batch(models)
+    b.set_tuning(4, 256, 0, 2)
+    b.set_persistent(persistent)
+    npers = b.persistent_members()
+    if persistent:
+        assert 0 < npers <= len(exps)     # the 32x32 member always qualifies
+    else:
+        assert npers == 0
+    b.integrate(2)
+    b.integrate(3)          # graphs and a single launch, both parities
+    for e, m, ref in zip(exps, models, alone):
+        sl = interior(e.n)
+        assert np.array_equal(m.get_state()[sl], ref[sl]), e.n
+    kernels = (npers > 0) + (npers < len(exps))
+    assert b.launch_count() == 5 * kernels
+    b.close()
+    for m in models:
+        m.close()
