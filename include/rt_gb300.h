@@ -207,11 +207,13 @@ const char* rt_batch_last_error(const rt_batch* b);
 int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph_steps);
 /* binary32 members whose x-y planes fill a CTA of `threads` consumer
  * threads (128/256/512; x and y extents multiples of 4) are stepped by the
- * batched warp-specialised kernel with every operand staged by bulk copies,
- * the others by the z-group / plane kernels; 0 puts every member in the
- * latter class.  Default 256.  No effect on results. */
+ * batched warp-specialised kernel with every operand staged by bulk copies;
+ * members with smaller planes (every axis z..m longer than one) by its form
+ * with several z slices per work item (256 or 512 consumer threads); the
+ * others by the z-group / plane kernels.  0 puts every member in the last
+ * class.  Default 256.  No effect on results. */
 int rt_batch_set_persistent(rt_batch* b, int threads);
-/* number of members in the warp-specialised class (negative: error) */
+/* number of members in the two warp-specialised classes (negative: error) */
 int rt_batch_persistent_members(rt_batch* b);
 /* advance every member by nsteps (asynchronous on the batch stream) */
 int rt_batch_integrate(rt_batch* b, int nsteps);

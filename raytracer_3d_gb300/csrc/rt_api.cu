@@ -268,6 +268,12 @@ struct rt_batch {
   long long* d_pfirst = nullptr;
   int pR = 0, pns = 0, pgrid = 0;
   long long pstage = 0;         // floats per stage
+  // members with small planes stepped by the z-slice staged kernel
+  int ns6 = 0;
+  void* d_smem6[2] = {nullptr, nullptr};
+  long long* d_sfirst = nullptr;
+  int sns = 0, sgrid = 0, sthreads = 0;
+  long long sstage = 0;
 };
 
 static int bfail(rt_batch* b, int code, const char* fmt, ...) {
@@ -294,7 +300,9 @@ static void batch_free_graphs(rt_batch* b) {
 }
 
 // kernel launches per batch step
-static int batch_kernels(const rt_batch* b) { return (b->np > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0); }
+static int batch_kernels(const rt_batch* b) {
+  return (b->np > 0 ? 1 : 0) + (b->ns6 > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0);
+}
 
 // one step of every member, starting from the arrays of parity `par`
 template <class T>
@@ -302,6 +310,8 @@ static cudaError_t batch_launch(rt_batch* b, int par) {
   cudaError_t e = cudaSuccess;
   if (b->np)
     e = launch_batch_w3(b->d_pmem[par], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage, b->pgrid, b->st);
+  if (e == cudaSuccess && b->ns6)
+    e = launch_batch_w6(b->d_smem6[par], b->d_sfirst, b->ns6, b->sthreads, b->sns, b->sstage, b->sgrid, b->st);
   if (e != cudaSuccess || !b->nq) return e;
   const void* mem = b->d_mem[par];
   const int n = b->nq;
@@ -371,10 +381,69 @@ static int batch_build_persistent(rt_batch* b, std::vector<int>& rest) {
   return RT_OK;
 }
 
+// binary32 members left over by the persistent class whose small planes fit
+// the z-slice staged kernel; its arrays, stage size and grid
+template <class T>
+static int batch_build_slices(rt_batch* b, std::vector<int>& rest) {
+  const int n = (int)b->mem.size();
+  b->ns6 = 0;
+  if (sizeof(T) != 4 || b->pthreads <= 0) return RT_OK;
+  const int nt = b->pthreads >= 256 ? b->pthreads : 256;
+  std::vector<int> sm, left;
+  std::vector<int> G;
+  long long stage = 0;
+  for (int j : rest) {
+    const int g = w6_slices(b->mem[j]->d, nt);
+    if (g > 0) {
+      sm.push_back(j);
+      G.push_back(g);
+      stage = std::max(stage, w6_stage_floats(b->mem[j]->d, g));
+    } else {
+      left.push_back(j);
+    }
+  }
+  const int ns = sm.empty() ? 0 : w6_stages(stage);
+  if (ns < 2) return RT_OK;
+  std::vector<BatchMember<float>> arr[2];
+  std::vector<long long> first(sm.size() + 1, 0);
+  for (size_t i = 0; i < sm.size(); i++) {
+    rt_handle* h = b->mem[sm[i]];
+    for (int par = 0; par < 2; par++) {
+      BatchMember<float> bm;
+      bm.A = make_step_args<float>(h, par == 0 ? h->cur : 1 - h->cur);
+      bm.S = make_sched(h->d, b->tune, G[i]);
+      arr[par].push_back(bm);
+    }
+    first[i + 1] = first[i] + (long long)((h->d.n[2] + G[i] - 1) / G[i]) * h->d.n[3] * h->d.n[4] * h->d.n[5];
+    b->cur0[sm[i]] = h->cur;
+  }
+  for (int par = 0; par < 2; par++) {
+    if (!b->d_smem6[par]) BCUDA_TRY(b, cudaMalloc(&b->d_smem6[par], (size_t)n * sizeof(BatchMember<float>)));
+    BCUDA_TRY(b, cudaMemcpy(b->d_smem6[par], arr[par].data(), sm.size() * sizeof(BatchMember<float>),
+                            cudaMemcpyHostToDevice));
+  }
+  if (!b->d_sfirst) BCUDA_TRY(b, cudaMalloc(&b->d_sfirst, (size_t)(n + 1) * sizeof(long long)));
+  BCUDA_TRY(b, cudaMemcpy(b->d_sfirst, first.data(), first.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  const int per_sm = w6_blocks_per_sm(nt, w6_smem(ns, stage));
+  if (per_sm < 1) return bfail(b, RT_ERR_CUDA, "batched z-slice kernel does not fit on an SM");
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  b->sgrid = (int)std::min<long long>(first.back(), (long long)per_sm * nsm);
+  b->sns = ns;
+  b->sstage = stage;
+  b->sthreads = nt;
+  b->ns6 = (int)sm.size();
+  rest = left;
+  return RT_OK;
+}
+
 template <class T>
 static int batch_build(rt_batch* b) {
   std::vector<int> qm;   // members of the plane / group / TMA class
   int rc = batch_build_persistent<T>(b, qm);
+  if (rc) return rc;
+  rc = batch_build_slices<T>(b, qm);
   if (rc) return rc;
   const int n = (int)qm.size();
   b->nq = n;
@@ -533,9 +602,11 @@ int rt_batch_destroy(rt_batch* b) {
   for (int k = 0; k < 2; k++) {
     cudaFree(b->d_mem[k]);
     cudaFree(b->d_pmem[k]);
+    cudaFree(b->d_smem6[k]);
   }
   cudaFree(b->d_first);
   cudaFree(b->d_pfirst);
+  cudaFree(b->d_sfirst);
   if (b->ev) cudaEventDestroy(b->ev);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
@@ -576,7 +647,7 @@ int rt_batch_persistent_members(rt_batch* b) {
     const int rc = b->fp64 ? batch_build<double>(b) : batch_build<float>(b);
     if (rc) return rc;
   }
-  return b->np;
+  return b->np + b->ns6;
 }
 
 int rt_batch_integrate(rt_batch* b, int nsteps) {
@@ -1062,7 +1133,7 @@ int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
       variant != RT_VARIANT_GROUP && variant != RT_VARIANT_PIPE && variant != RT_VARIANT_WS &&
       variant != RT_VARIANT_WSD && variant != RT_VARIANT_W2 && variant != RT_VARIANT_W2D &&
       variant != RT_VARIANT_W3 && variant != RT_VARIANT_W4 && variant != RT_VARIANT_W5 &&
-      variant != RT_VARIANT_W5H)
+      variant != RT_VARIANT_W5H && variant != RT_VARIANT_W6)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
   if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)

@@ -66,6 +66,7 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_W4 10
 #define RT_VARIANT_W5 11
 #define RT_VARIANT_W5H 12
+#define RT_VARIANT_W6 13
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule
@@ -114,6 +115,16 @@ int batch_w3_stages(long long stage_floats);
 size_t batch_w3_smem(int ns, long long stage_floats);
 int batch_w3_blocks_per_sm(int threads, int R, size_t smem);
 cudaError_t launch_batch_w3(const void* members, const long long* first, int nmem, int threads, int R, int ns,
+                            long long stage_floats, int grid, cudaStream_t st);
+// small-plane staged kernel (rt_persist.cu): z slices per item for a CTA
+// of `threads` consumers (0: the field does not fit it), stage size,
+// stages, shared memory, residency and the batched launch
+int w6_slices(const Dims& d, int threads);
+long long w6_stage_floats(const Dims& d, int G);
+int w6_stages(long long stage_floats);
+size_t w6_smem(int ns, long long stage_floats);
+int w6_blocks_per_sm(int threads, size_t smem);
+cudaError_t launch_batch_w6(const void* members, const long long* first, int nmem, int threads, int ns,
                             long long stage_floats, int grid, cudaStream_t st);
 // persistent binary32 kernels (rt_persist.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them

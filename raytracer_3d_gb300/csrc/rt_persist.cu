@@ -6,12 +6,14 @@
 // the form with every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3),
 // the form with the producer folded into warp 0 (rt_step9.cuh,
 // RT_VARIANT_W4), and the row-chunk form with consumer groups (rt_step10.cuh,
-// RT_VARIANT_W5 with 256-thread groups, RT_VARIANT_W5H with 128).
+// RT_VARIANT_W5 with 256-thread groups, RT_VARIANT_W5H with 128), and the
+// small-plane form with z slices per item (rt_step11.cuh, RT_VARIANT_W6,
+// also for the ensemble class of small planes).
 // Kept in a translation unit of their own so the library builds in parallel.
 #include <algorithm>
 
 #include "rt_kernels.h"
-#include "rt_step10.cuh"
+#include "rt_step11.cuh"
 
 namespace rt {
 
@@ -315,7 +317,64 @@ int bw3_per_sm_nt(int R, size_t smem) {
   return e == cudaSuccess ? per_sm : 0;
 }
 
+template <int NT>
+int w6_per_sm_nt(size_t smem) {
+  int per_sm = 0;
+  set_smem(step_w6_kernel<NT>, smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_w6_kernel<NT>, NT + 32, smem) != cudaSuccess)
+    return 0;
+  return per_sm;
+}
+
+template <int NT>
+cudaError_t launch_w6_nt(const StepArgs<float>& A, const PlaneSched& S, const void* members,
+                         const long long* first, int nmem, long long nitems, int ns, long long stage_floats,
+                         int grid, cudaStream_t st) {
+  const size_t sm = w6_head_bytes() + (size_t)ns * stage_floats * sizeof(float);
+  cudaError_t e = set_smem(step_w6_kernel<NT>, sm);
+  if (e != cudaSuccess) return e;
+  step_w6_kernel<NT><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, static_cast<const BatchMember<float>*>(members),
+                                                          first, nmem, nitems, ns, stage_floats);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+// ---- small-plane staged kernel ----
+int w6_slices(const Dims& d, int threads) {
+  if (threads != 256 && threads != 512) return 0;
+  const int nx = d.n[0], ny = d.n[1];
+  if (nx < 4 || nx % 4 || ny < 4 || ny % 4) return 0;
+  for (int a = 2; a < 6; a++)
+    if (d.n[a] < 2) return 0;
+  const long long P = (long long)nx * ny;
+  int G = (int)(2LL * threads / P);
+  if (G > RT_W6_MAXG) G = RT_W6_MAXG;
+  if (G > d.n[2]) G = d.n[2];
+  if (G < 1) return 0;
+  // at least half of the consumer threads own cells
+  if (2 * (G * P / 2) < threads) return 0;
+  if (w6_items(d, G) >= (1LL << 31)) return 0;
+  return G;
+}
+long long w6_stage_floats(const Dims& d, int G) { return (long long)w6_layout(d, G).floats(); }
+int w6_stages(long long stage_floats) {
+  const long long room = (long long)ws_max_smem() - (long long)w6_head_bytes();
+  const long long ns = room > 0 ? room / (stage_floats * (long long)sizeof(float)) : 0;
+  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
+}
+size_t w6_smem(int ns, long long stage_floats) { return w6_head_bytes() + (size_t)ns * stage_floats * sizeof(float); }
+int w6_blocks_per_sm(int threads, size_t smem) {
+  return threads == 256 ? w6_per_sm_nt<256>(smem) : w6_per_sm_nt<512>(smem);
+}
+cudaError_t launch_batch_w6(const void* members, const long long* first, int nmem, int threads, int ns,
+                            long long stage_floats, int grid, cudaStream_t st) {
+  StepArgs<float> A{};   // unused: the members carry their arguments
+  PlaneSched S{};
+  if (threads == 256)
+    return launch_w6_nt<256>(A, S, members, first, nmem, -1, ns, stage_floats, grid, st);
+  return launch_w6_nt<512>(A, S, members, first, nmem, -1, ns, stage_floats, grid, st);
+}
 
 // ---- batched form of the fully staged kernel ----
 int batch_w3_rows(const Dims& d, int threads, int R_class) {
@@ -354,6 +413,22 @@ cudaError_t launch_batch_w3(const void* members, const long long* first, int nme
 
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
   done = false;
+  if (tn.variant == RT_VARIANT_W6 && w6_slices(A.d, tn.threads) > 0) {
+    const int G = w6_slices(A.d, tn.threads);
+    const long long sf = w6_stage_floats(A.d, G);
+    const int ns = w6_stages(sf);
+    if (ns >= 2) {
+      done = true;
+      const PlaneSched S = make_sched(A.d, tn, G);
+      const size_t sm = w6_smem(ns, sf);
+      const int per_sm = w6_blocks_per_sm(tn.threads, sm);
+      if (per_sm < 1) return cudaErrorInvalidConfiguration;
+      const long long nitems = w6_items(A.d, G);
+      const int grid = (int)std::min<long long>(nitems, (long long)per_sm * sm_count());
+      if (tn.threads == 256) return launch_w6_nt<256>(A, S, nullptr, nullptr, 0, nitems, ns, sf, grid, st);
+      return launch_w6_nt<512>(A, S, nullptr, nullptr, 0, nitems, ns, sf, grid, st);
+    }
+  }
   if (tn.variant == RT_VARIANT_W5 && w5_ok(A.d, 256, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);

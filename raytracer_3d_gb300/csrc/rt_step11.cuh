@@ -1,0 +1,393 @@
+// rt_step11.cuh -- warp-specialised staged step for small x-y planes:
+// G consecutive z slices per work item (binary32 form).
+//
+// For planes of a few hundred cells a CTA of NT consumer threads (2 cells
+// each) would idle on one plane, so a work item is G = 2*NT/(nx*ny) slices
+// z0 .. z0+G-1 of one (k,l,m), in band order over (l,m) with (z group, k)
+// inside (PlaneSched with gz = G).  A stage holds all that the G slices
+// read, each piece one bulk copy of a whole plane (or face-0 row), issued by
+// the producer warp, 32 copies at a time:
+//   E at z0-2 .. z0+G+1 (boundary maps applied per plane; the z window is
+//   shared by the slices), the 12 k,l,m neighbour planes of every slice,
+//   the 11 velocity / rate planes of every slice, the face-0 rows of every
+//   slice.
+// Consumer thread t owns the cell pair (x0, x0+1) of row y of slice g, with
+// x faces passed between lanes by shuffle.  Slices past nz (last group) are
+// computed from clamped planes and not stored.  The arithmetic per face and
+// per cell (flux_fp32, axis order x,y,z,k,l,m, divergence, update) is that
+// of the other binary32 kernels: results are bit-identical to them.
+// Requires nx, ny multiples of 4 and every axis z..m longer than one.
+// The same kernel steps one field or, over a member list, an ensemble.
+#pragma once
+#include "rt_step10.cuh"
+
+namespace rt {
+
+#define RT_W6_MAXG 16
+
+struct W6Desc {
+  long long p0;   // cell (0,0) of slice z0
+  int member, z0;
+  float kr[4], ki[4], kl[4];                              // k,l,m faces (index a-2)
+  float zr[RT_W6_MAXG], zi[RT_W6_MAXG], zl[RT_W6_MAXG];  // z faces of every slice
+};
+__host__ __device__ constexpr size_t w6_desc_bytes() { return (sizeof(W6Desc) + 15) / 16 * 16; }
+__host__ __device__ constexpr size_t w6_head_bytes() { return 128 + RT_WS_MAXSTAGE * w6_desc_bytes(); }
+
+struct W6Layout {
+  int P, G, nx, ny;
+  __host__ __device__ int ez(int zz) const { return zz * P; }   // zz = z - z0 + 2
+  __host__ __device__ int en(int g, int a, int i) const { return (G + 4 + g * 12 + (a - 3) * 4 + i) * P; }
+  // v: 0 x, 1 y, 2..5 right faces of z..m, 6..9 left faces of z..m, 10 rate
+  __host__ __device__ int v(int g, int k) const { return (G + 4 + 12 * G + g * 11 + k) * P; }
+  __host__ __device__ int b0x(int g) const { return (24 * G + 4) * P + g * (nx + ny); }
+  __host__ __device__ int b0y(int g) const { return b0x(g) + ny; }
+  __host__ __device__ int floats() const { return (24 * G + 4) * P + G * (nx + ny); }
+  // z window G+4, k,l,m neighbours 12G, velocities and rate 11G, face-0 rows 2G
+  __host__ __device__ int copies() const { return 26 * G + 4; }
+};
+
+__host__ __device__ __forceinline__ W6Layout w6_layout(const Dims& d, int G) {
+  return W6Layout{d.n[0] * d.n[1], G, d.n[0], d.n[1]};
+}
+
+// copy j of an item: what it holds and where it lands in the stage
+struct W6Copy {
+  int kind;        // 0 z window, 1 k/l/m neighbour, 2 velocity or rate, 3 face-0 row
+  int g, a, i;     // slice; axis or plane index; offset index / row (0 x, 1 y)
+  int dst;         // stage offset, floats
+  unsigned bytes;
+};
+__host__ __device__ __forceinline__ W6Copy w6_copy(const W6Layout& L, int j) {
+  W6Copy c{0, 0, 0, 0, 0, (unsigned)(L.P * sizeof(float))};
+  const int G = L.G;
+  if (j < G + 4) {
+    c.kind = 0;
+    c.i = j;
+    c.dst = L.ez(j);
+    return c;
+  }
+  int jj = j - (G + 4);
+  if (jj < 12 * G) {
+    c.kind = 1;
+    c.g = jj / 12;
+    c.a = 3 + (jj % 12) / 4;
+    c.i = jj % 4;
+    c.dst = L.en(c.g, c.a, c.i);
+    return c;
+  }
+  jj -= 12 * G;
+  if (jj < 11 * G) {
+    c.kind = 2;
+    c.g = jj / 11;
+    c.a = jj % 11;
+    c.dst = L.v(c.g, c.a);
+    return c;
+  }
+  jj -= 11 * G;
+  c.kind = 3;
+  c.g = jj / 2;
+  c.i = jj % 2;
+  c.dst = c.i == 0 ? L.b0x(c.g) : L.b0y(c.g);
+  c.bytes = (unsigned)((c.i == 0 ? L.ny : L.nx) * sizeof(float));
+  return c;
+}
+// bytes the item's mbarrier expects: the sum of w6_copy(L, j).bytes
+__host__ __device__ __forceinline__ unsigned w6_tx_bytes(const W6Layout& L) {
+  return (unsigned)((L.G + 4 + 23 * L.G) * L.P * sizeof(float) + L.G * (L.nx + L.ny) * sizeof(float));
+}
+
+// item -> (z0, k, l, m) for z groups of G slices (band order of rt_step6.cuh)
+__device__ __forceinline__ void w6_decode(const Dims& d, const PlaneSched& S, unsigned item, int c[6]) {
+  const unsigned ngz = (unsigned)((d.n[2] + S.gz - 1) / S.gz);
+  const unsigned nb_axis = S.sweep ? d.n[4] : d.n[5];
+  const unsigned no_axis = S.sweep ? d.n[5] : d.n[4];
+  const unsigned nunits = (unsigned)S.nunits;
+  const unsigned per_full = nunits * no_axis * (unsigned)S.band;
+  const unsigned b = item / per_full;
+  unsigned rem = item - b * per_full;
+  unsigned bsize = S.band;
+  if ((b + 1) * (unsigned)S.band > nb_axis) bsize = nb_axis - b * (unsigned)S.band;
+  const unsigned u = rem % nunits;
+  rem /= nunits;
+  const unsigned inner = rem % bsize;
+  const unsigned outer = rem / bsize;
+  const int banded = (int)(b * (unsigned)S.band + inner);
+  c[0] = 0;
+  c[1] = 0;
+  c[2] = (int)(u % ngz) * S.gz;
+  c[3] = (int)(u / ngz);
+  c[4] = S.sweep ? banded : (int)outer;
+  c[5] = S.sweep ? (int)outer : banded;
+}
+
+__host__ __device__ __forceinline__ long long w6_items(const Dims& d, int G) {
+  return (long long)((d.n[2] + G - 1) / G) * d.n[3] * d.n[4] * d.n[5];
+}
+
+// one item into a stage, by the 32 lanes of the producer warp
+__device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSched& S, long long li, int member,
+                                         float* sP, W6Desc* D, uint64_t* fullb, uint64_t* dfulb) {
+  const Dims& d = A.d;
+  const int lane = threadIdx.x & 31;
+  const int G = S.gz;
+  const W6Layout L = w6_layout(d, G);
+  const int nz = d.n[2];
+  int c[6];
+  w6_decode(d, S, (unsigned)li, c);
+  const int z0 = c[2];
+  const long long p0 = (long long)z0 * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+                       (long long)c[5] * d.s[5];
+  if (lane == 0) {
+    D->p0 = p0;
+    D->member = member;
+    D->z0 = z0;
+#pragma unroll
+    for (int a = 3; a < 6; a++) {
+      D->kr[a - 2] = A.t32.hcfl[a][pidx(c[a] + 1)];
+      D->ki[a - 2] = A.t32.inv_d[a][pidx(c[a] + 1)];
+      D->kl[a - 2] = A.t32.hcfl[a][pidx(c[a])];
+    }
+    for (int g = 0; g < G; g++) {
+      const int z = z0 + g < nz ? z0 + g : nz - 1;
+      D->zr[g] = A.t32.hcfl[2][pidx(z + 1)];
+      D->zi[g] = A.t32.inv_d[2][pidx(z + 1)];
+      D->zl[g] = A.t32.hcfl[2][pidx(z)];
+    }
+    mbar_arrive(dfulb);
+    mbar_arrive_expect_tx(fullb, w6_tx_bytes(L));
+  }
+  __syncwarp();
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const int ncopy = L.copies();
+  for (int j = lane; j < ncopy; j += 32) {
+    const W6Copy cp = w6_copy(L, j);
+    const float* src;
+    if (cp.kind == 0) {
+      // the shared z window; rows past nz+1 only feed slices past nz
+      int za = z0 - 2 + cp.i;
+      if (za > nz + 1) za = nz + 1;
+      int flip = 0;
+      const int zm = map_coord(d, 2, za, flip);
+      const int m = flip ? d.n[5] - 1 - c[5] : c[5];
+      src = A.E + ((long long)zm * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+                   (long long)m * d.s[5]);
+    } else {
+      int cg[6] = {0, 0, c[2], c[3], c[4], c[5]};
+      cg[2] = z0 + cp.g < nz ? z0 + cp.g : nz - 1;
+      if (cp.kind == 1) {
+        src = A.E + nb_plane(d, cg, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1);
+      } else if (cp.kind == 2) {
+        const long long pg = p0 + (long long)(cg[2] - z0) * d.s[2];
+        const int k = cp.a;
+        if (k < 6) {
+          src = A.vel[k] + pg;
+        } else if (k < 10) {
+          const int a = k - 4;
+          if (cg[a] > 0) {
+            src = A.vel[a] + (pg - d.s[a]);
+          } else {
+            long long off = 0;
+#pragma unroll
+            for (int b = 2; b < 6; b++) off += (long long)cg[b] * d.ps[a][b];
+            src = A.vlo[a] + off;
+          }
+        } else {
+          src = A.lam[0] + pg;
+        }
+      } else {
+        long long off = 0;   // face-0 x row (by y) or face-0 y row (by x) of the slice
+#pragma unroll
+        for (int b = 2; b < 6; b++) off += (long long)cg[b] * d.ps[cp.i][b];
+        src = A.vlo[cp.i] + off;
+      }
+    }
+    bulk_g2s(sP + cp.dst, src, cp.bytes, fullb);
+  }
+}
+
+// a consumer thread's cell pair and its constants, fixed for one field
+struct W6Geom {
+  int nx, ny, P, G, g, y, x0, xm, xmm;
+  bool has_right, active;
+  float cxa, cxb, ixa, ixb, cxl, cy, iy, cyb, dt;
+};
+
+__device__ __forceinline__ void w6_geom(const StepArgs<float>& A, int G, int t, W6Geom& w) {
+  const int nx = A.d.n[0], ny = A.d.n[1];
+  w.nx = nx;
+  w.ny = ny;
+  w.P = nx * ny;
+  w.G = G;
+  const int hx = nx >> 1, ts = hx * ny;   // threads per slice
+  int g = t / ts;
+  w.active = g < G;
+  if (!w.active) g = G - 1;
+  const int rem = t % ts;
+  w.g = g;
+  w.y = rem / hx;
+  w.x0 = 2 * (rem % hx);
+  const int x0 = w.x0, y = w.y;
+  w.xm = x0 > 0 ? x0 - 1 : 0;
+  w.xmm = x0 > 1 ? x0 - 2 : 0;
+  w.has_right = x0 + 2 < nx;
+  w.cxa = A.t32.hcfl[0][pidx(x0 + 1)];
+  w.cxb = A.t32.hcfl[0][pidx(x0 + 2)];
+  w.ixa = A.t32.inv_d[0][pidx(x0 + 1)];
+  w.ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  w.cxl = A.t32.hcfl[0][pidx(x0)];
+  w.cy = A.t32.hcfl[1][pidx(y + 1)];
+  w.iy = A.t32.inv_d[1][pidx(y + 1)];
+  w.cyb = A.t32.hcfl[1][pidx(y)];
+  w.dt = (float)A.dt;
+}
+
+__device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& w, const W6Desc& D,
+                                        const float* sP, int lane) {
+  const Dims& d = A.d;
+  const int nx = w.nx, ny = w.ny, x0 = w.x0, y = w.y, g = w.g;
+  const W6Layout L{w.P, w.G, nx, ny};
+  const float* sC = sP + L.ez(g + 2);   // the slice's own E plane
+  float2 ec[5];
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    int yy = y + j - 2;
+    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
+    ec[j] = ld2(sC + yy * nx + x0);
+  }
+  const int q = y * nx + x0;
+  // ---- x faces ----
+  const float* row = sC + y * nx;
+  const float2 e01 = ec[2];
+  const float2 e23 = w.has_right ? ld2(row + x0 + 2) : make_float2(e01.y, e01.y);
+  const float2 vx = ld2(sP + L.v(g, 0) + q);
+  const float fxa = flux_fp32(vx.x, w.cxa, row[w.xm], e01.x, e01.y, e23.x);
+  const float fxb = flux_fp32(vx.y, w.cxb, e01.x, e01.y, e23.x, e23.y);
+  float fxl = __shfl_up_sync(0xffffffffu, fxb, 1);
+  if (x0 == 0)
+    fxl = open_face0_flux<float>(sP[L.b0x(g) + y], e01.x);
+  else if (lane == 0)
+    fxl = flux_fp32(sP[L.v(g, 0) + q - 1], w.cxl, row[w.xmm], row[x0 - 1], e01.x, e01.y);
+  // ---- y faces ----
+  float2 fyb, fyt;
+  if (y == 0) {
+    const float2 vb = ld2(sP + L.b0y(g) + x0);
+    fyb.x = open_face0_flux<float>(vb.x, e01.x);
+    fyb.y = open_face0_flux<float>(vb.y, e01.y);
+  } else {
+    const float2 vb = ld2(sP + L.v(g, 1) + q - nx);
+    fyb.x = flux_fp32(vb.x, w.cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
+    fyb.y = flux_fp32(vb.y, w.cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
+  }
+  {
+    const float2 vy = ld2(sP + L.v(g, 1) + q);
+    fyt.x = flux_fp32(vy.x, w.cy, ec[1].x, ec[2].x, ec[3].x, ec[4].x);
+    fyt.y = flux_fp32(vy.y, w.cy, ec[1].y, ec[2].y, ec[3].y, ec[4].y);
+  }
+  // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
+  const float2 e0 = e01;
+  float dEa = 0.f, dEb = 0.f;
+  dEa -= (fxa - fxl) * w.ixa;
+  dEb -= (fxb - fxa) * w.ixb;
+  dEa -= (fyt.x - fyb.x) * w.iy;
+  dEb -= (fyt.y - fyb.y) * w.iy;
+  {
+    const float2 Em2 = ld2(sP + L.ez(g) + q), Em1 = ld2(sP + L.ez(g + 1) + q);
+    const float2 Ep1 = ld2(sP + L.ez(g + 3) + q), Ep2 = ld2(sP + L.ez(g + 4) + q);
+    const float2 vr = ld2(sP + L.v(g, 2) + q), vl = ld2(sP + L.v(g, 6) + q);
+    const float cr = D.zr[g], ci = D.zi[g], cl = D.zl[g];
+    const float fra = flux_fp32(vr.x, cr, Em1.x, e0.x, Ep1.x, Ep2.x);
+    const float fla = flux_fp32(vl.x, cl, Em2.x, Em1.x, e0.x, Ep1.x);
+    dEa -= (fra - fla) * ci;
+    const float frb = flux_fp32(vr.y, cr, Em1.y, e0.y, Ep1.y, Ep2.y);
+    const float flb = flux_fp32(vl.y, cl, Em2.y, Em1.y, e0.y, Ep1.y);
+    dEb -= (frb - flb) * ci;
+  }
+#pragma unroll
+  for (int a = 3; a < 6; a++) {
+    const float2 Em2 = ld2(sP + L.en(g, a, 0) + q), Em1 = ld2(sP + L.en(g, a, 1) + q);
+    const float2 Ep1 = ld2(sP + L.en(g, a, 2) + q), Ep2 = ld2(sP + L.en(g, a, 3) + q);
+    const float2 vr = ld2(sP + L.v(g, a) + q), vl = ld2(sP + L.v(g, a + 4) + q);
+    const float cr = D.kr[a - 2], ci = D.ki[a - 2], cl = D.kl[a - 2];
+    const float fra = flux_fp32(vr.x, cr, Em1.x, e0.x, Ep1.x, Ep2.x);
+    const float fla = flux_fp32(vl.x, cl, Em2.x, Em1.x, e0.x, Ep1.x);
+    dEa -= (fra - fla) * ci;
+    const float frb = flux_fp32(vr.y, cr, Em1.y, e0.y, Ep1.y, Ep2.y);
+    const float flb = flux_fp32(vl.y, cl, Em2.y, Em1.y, e0.y, Ep1.y);
+    dEb -= (frb - flb) * ci;
+  }
+  const float2 lam = ld2(sP + L.v(g, 10) + q);
+  const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
+  if (w.active && D.z0 + g < d.n[2])
+    st2_stream(A.Enew + D.p0 + (long long)g * d.s[2] + q,
+               make_float2(e0.x + w.dt * (dEa - mfa), e0.y + w.dt * (dEb - mfb)));
+}
+
+// one field (mem == nullptr: A, S, nitems) or the members of an ensemble
+// (member j owns items [first[j], first[j+1]), its slices per item in
+// mem[j].S.gz; nitems = first[nmem])
+template <int NT>
+__global__ void __launch_bounds__(NT + 32, 1)
+    step_w6_kernel(StepArgs<float> A, PlaneSched S, const BatchMember<float>* __restrict__ mem,
+                   const long long* __restrict__ first, int nmem, long long nitems, int ns, long long stage_floats) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* empty = full + RT_WS_MAXSTAGE;
+  uint64_t* dful = empty + RT_WS_MAXSTAGE;
+  W6Desc* desc = reinterpret_cast<W6Desc*>(smem_raw + 128);
+  float* stage0 = reinterpret_cast<float*>(smem_raw + w6_head_bytes());
+  int* status = mem ? mem[0].A.status : A.status;
+  if (mem) nitems = first[nmem];
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ns; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NT);
+      mbar_init(&dful[s], 1);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (blockIdx.x >= nitems) return;
+
+  if (threadIdx.x >= NT) {
+    int s = 0, j = 0;
+    uint32_t rnd = 0;
+    long long issued = 0;
+    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
+      if (mem) {
+        while (it >= first[j + 1]) j++;
+        w6_issue(mem[j].A, mem[j].S, it - first[j], j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s],
+                 &dful[s]);
+      } else {
+        w6_issue(A, S, it, 0, stage0 + (size_t)s * stage_floats, &desc[s], &full[s], &dful[s]);
+      }
+      issued++;
+      if (++s == ns) { s = 0; rnd++; }
+    }
+    ws_drain(full, ns, issued);
+    return;
+  }
+
+  const int lane = threadIdx.x & 31;
+  W6Geom w;
+  int jc = -1;
+  int s = 0;
+  uint32_t par = 0;
+  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    if (!ws_wait(&dful[s], par, status)) return;
+    const int j = desc[s].member;
+    const StepArgs<float>& Aj = mem ? mem[j].A : A;
+    if (j != jc) {
+      w6_geom(Aj, mem ? mem[j].S.gz : S.gz, threadIdx.x, w);
+      jc = j;
+    }
+    if (!ws_wait(&full[s], par, status)) return;
+    w6_item(Aj, w, desc[s], stage0 + (size_t)s * stage_floats, lane);
+    mbar_arrive(&empty[s]);
+    if (++s == ns) { s = 0; par ^= 1u; }
+  }
+}
+
+}  // namespace rt

@@ -33,6 +33,57 @@ __host__ __device__ __forceinline__ size_t w3_smem(const Dims& d, int ns) {
   return ws_head_bytes() + (size_t)ns * w3_stage_floats(d) * sizeof(float);
 }
 
+// copy `lane` of an item (0..29): what it holds and where it lands
+struct W3Copy {
+  bool valid;      // false: the axis is collapsed (no copy)
+  int kind;        // 0 E plane, 1 right-face velocities, 2 left-face velocities, 3 x/y velocity or rate, 4 face-0 row
+  int a, i;        // axis and neighbour index (kind 0), axis (1, 2), which (3: 0 x, 1 y, 2 rate; 4: 0 x, 1 y)
+  long long dst;   // stage offset, floats
+  unsigned bytes;
+};
+__host__ __device__ __forceinline__ W3Copy w3_copy(const Dims& d, int lane) {
+  const int nx = d.n[0], ny = d.n[1];
+  const long long nxy = (long long)nx * ny;
+  W3Copy c{false, 0, 0, 0, 0, (unsigned)(nxy * sizeof(float))};
+  if (lane < RT_NPLANE) {
+    c.kind = 0;
+    if (lane == 0) {
+      c.valid = true;
+    } else {
+      c.a = 2 + (lane - 1) / 4;
+      c.i = (lane - 1) % 4;
+      c.valid = d.n[c.a] > 1;
+    }
+    c.dst = lane * nxy;
+  } else if (lane < 25) {
+    const bool right = lane < 21;
+    c.kind = right ? 1 : 2;
+    c.a = 2 + (right ? lane - 17 : lane - 21);
+    c.valid = d.n[c.a] > 1;
+    c.dst = (long long)((right ? RT_W3_VR : RT_W3_VL) + c.a - 2) * nxy;
+  } else if (lane < 28) {
+    c.kind = 3;
+    c.i = lane - 25;
+    c.valid = true;
+    c.dst = (long long)(c.i == 0 ? RT_W3_VX : (c.i == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
+  } else if (lane < 30) {
+    c.kind = 4;
+    c.i = lane - 28;
+    c.valid = true;
+    c.dst = (long long)RT_W3_NPL * nxy + (c.i == 0 ? 0 : ny);
+    c.bytes = (unsigned)((c.i == 0 ? ny : nx) * sizeof(float));
+  }
+  return c;
+}
+// bytes the item's mbarrier expects: the sum of the valid copies' bytes
+__host__ __device__ __forceinline__ unsigned w3_tx_bytes(const Dims& d) {
+  unsigned nact = 0;
+  for (int a = 2; a < 6; a++)
+    if (d.n[a] > 1) nact++;
+  const unsigned pbytes = (unsigned)((long long)d.n[0] * d.n[1] * sizeof(float));
+  return (1 + 6 * nact + 3) * pbytes + (unsigned)((d.n[0] + d.n[1]) * sizeof(float));
+}
+
 // One item into stage s, by the 32 lanes of a warp: all lanes decode it,
 // lane 0 publishes the descriptor and arms the stage, lane j issues copy j:
 // 0..16 the E planes (as rt_step6.cuh), 17..20 right and 21..24 left face
@@ -43,14 +94,11 @@ __device__ __forceinline__ void w3_issue(const StepArgs<float>& A, const PlaneSc
                                          float* sP, WsDesc* D, uint64_t* fullb, uint64_t* dfulb) {
   const Dims& d = A.d;
   const int lane = threadIdx.x & 31;
-  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
-  const uint32_t pbytes = (uint32_t)(nxy * sizeof(float));
   int c[6];
   ws_decode(d, S, (unsigned)li, c);
   const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                        (long long)c[5] * d.s[5];
   if (lane == 0) {
-    uint32_t nact = 0;
     D->p0 = p0;
     D->member = member;
 #pragma unroll
@@ -59,58 +107,37 @@ __device__ __forceinline__ void w3_issue(const StepArgs<float>& A, const PlaneSc
       D->kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
       D->kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
       D->kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
-      if (act) nact++;
     }
     mbar_arrive(dfulb);
-    // E centre + 4 neighbours and 2 velocity planes per active axis, x/y
-    // velocities, rate, and the two face-0 rows
-    mbar_arrive_expect_tx(fullb, (1 + 6 * nact + 3) * pbytes + (uint32_t)((nx + ny) * sizeof(float)));
+    mbar_arrive_expect_tx(fullb, w3_tx_bytes(d));
   }
   __syncwarp();
-  const float* src = nullptr;
-  float* dst = nullptr;
-  uint32_t bytes = pbytes;
-  if (lane < RT_NPLANE) {
-    long long off = p0;
-    bool go = true;
-    if (lane > 0) {
-      const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
-      go = d.n[a] > 1;
-      if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
-    }
-    if (go) { src = A.E + off; dst = sP + (size_t)lane * nxy; }
-  } else if (lane < 25) {
-    const bool right = lane < 21;
-    const int a = 2 + (right ? lane - 17 : lane - 21);
-    if (d.n[a] > 1) {
-      if (right) {
-        src = A.vel[a] + p0;
-      } else if (c[a] > 0) {
-        src = A.vel[a] + (p0 - d.s[a]);
+  const W3Copy cp = w3_copy(d, lane);
+  if (lane < 30 && cp.valid) {
+    const float* src;
+    if (cp.kind == 0) {
+      src = A.E + (lane == 0 ? p0 : nb_plane(d, c, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1));
+    } else if (cp.kind == 1) {
+      src = A.vel[cp.a] + p0;
+    } else if (cp.kind == 2) {
+      if (c[cp.a] > 0) {
+        src = A.vel[cp.a] + (p0 - d.s[cp.a]);
       } else {
         long long off = 0;
 #pragma unroll
-        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-        src = A.vlo[a] + off;
+        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.a][b];
+        src = A.vlo[cp.a] + off;
       }
-      dst = sP + (size_t)((right ? RT_W3_VR : RT_W3_VL) + a - 2) * nxy;
-    }
-  } else if (lane < 28) {
-    const int which = lane - 25;   // x velocity, y velocity, rate
-    src = (which == 0 ? A.vel[0] : (which == 1 ? A.vel[1] : A.lam[0])) + p0;
-    dst = sP + (size_t)(which == 0 ? RT_W3_VX : (which == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
-  } else if (lane < 30) {
-    long long off = 0;
-    const int a = lane - 28;   // face-0 x row (by y), face-0 y row (by x)
+    } else if (cp.kind == 3) {
+      src = (cp.i == 0 ? A.vel[0] : (cp.i == 1 ? A.vel[1] : A.lam[0])) + p0;
+    } else {
+      long long off = 0;   // face-0 x row (by y), face-0 y row (by x)
 #pragma unroll
-    for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-    src = A.vlo[a] + off;
-    dst = sP + (size_t)RT_W3_NPL * nxy + (a == 0 ? 0 : ny);
-    bytes = (uint32_t)((a == 0 ? ny : nx) * sizeof(float));
-  }
-  if (src) {
+      for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.i][b];
+      src = A.vlo[cp.i] + off;
+    }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    bulk_g2s(dst, src, bytes, fullb);
+    bulk_g2s(sP + cp.dst, src, cp.bytes, fullb);
   }
 }
 

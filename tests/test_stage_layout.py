@@ -1,0 +1,36 @@
+"""The staged binary32 kernels arm each stage's mbarrier with the byte
+count of the copies they issue; a mismatch leaves the barrier incomplete
+(the kernel then times out and reports an error).  This compiles the
+kernels' own copy-list code for the host and checks, over a sweep of
+shapes, that expected and copied bytes agree, that every copy lands inside
+its stage without overlap, and that all copies are 16-byte aligned."""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(ROOT, "raytracer_3d_gb300", "csrc")
+
+
+def _nvcc():
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        pytest.skip("nvcc not available")
+    return exe
+
+
+def test_stage_copy_lists_match_barrier_bytes():
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "stage_layout_check")
+        cmd = [_nvcc(), "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC,
+               "-I", os.path.join(ROOT, "include"), os.path.join(HERE, "native", "stage_layout_check.cu"), "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+        print(r.stdout)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert "0 failures" in r.stdout
