@@ -224,7 +224,7 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
     return out
 
 
-def bench_batched(steps, warmup, members=48, seed=2024):
+def bench_batched(steps, warmup, members=48, seed=2024, fixed=None):
     """48 independent fp32 instances (dims per axis from {8,16,24,32} spatial
     and {8,12,16,24} spectral, own N0, f, mean-flow amplitude, packet init)
     advanced by one persistent, graph-captured launch per step, with the
@@ -244,7 +244,12 @@ def bench_batched(steps, warmup, members=48, seed=2024):
         models.append(m)
     setup_s = time.perf_counter() - t0
     b = Batch(models)
-    best, table = tune_batch(b, reps=2, use_cache=False)
+    if fixed:   # band, threads, sweep, persistent threads (profiling runs)
+        b.set_tuning(fixed[0], fixed[1], fixed[2], 16)
+        b.set_persistent(fixed[3])
+        best = tuple(fixed)
+    else:
+        best, table = tune_batch(b, reps=2, use_cache=False)
     b.integrate(warmup)
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream())
@@ -278,7 +283,7 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
     fp64 one-at-a-time baseline on the first requests."""
     from raytracer_3d_gb300.serve import GpuExecutor, SequentialExecutor, Server, poisson_requests
     reqs = poisson_requests(nreq, rate=rate, seed=seed)
-    ex = GpuExecutor("fp32", batch_tuning=(8, 1024, 0, 16))
+    ex = GpuExecutor("fp32", batch_tuning=(8, 512, 1, 16), persistent=512)
     rep = Server(ex, budget_bytes=budget, chunk_max=50).run(reqs)
     ex.close()
     s = rep.summary()
@@ -311,6 +316,12 @@ def gpu_arm(args):
     rank, world, local, dist = dist_init(args.gpus)
     n = tuple(int(v) for v in args.dims.split(",")) if args.dims else (args.n,) * 6
     sched = (args.variant, args.band, args.threads, args.sweep)
+    if args.only == "batch":   # profiling runs of the batched form only
+        out = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,
+                            fixed=tuple(int(v) for v in args.batch_tuning.split(",")) if args.batch_tuning else None)
+        if rank == 0:
+            print(json.dumps({"profile_only": "fp32_batched", **out}), flush=True)
+        return
     if args.no_fp64:  # profiling runs of the fp32 form only
         f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
         if rank == 0:
@@ -333,7 +344,7 @@ def gpu_arm(args):
                          "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
                          "clocks": f32["clocks"]}
     if not args.no_batch:
-        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup)
+        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup, members=args.batch_members)
     if not args.no_serve:
         forms["serving"] = bench_serving(nreq=args.serve_requests)
     cells = main["cells"]
@@ -402,6 +413,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--batch-members", type=int, default=48)
+    ap.add_argument("--batch-tuning", default=None, help="band,threads,sweep,persistent (skip the batch tuner)")
+    ap.add_argument("--only", default="all", choices=("all", "batch"), help="batch: the batched form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -34,67 +34,100 @@ struct W6Desc {
 __host__ __device__ constexpr size_t w6_desc_bytes() { return (sizeof(W6Desc) + 15) / 16 * 16; }
 __host__ __device__ constexpr size_t w6_head_bytes() { return 128 + RT_WS_MAXSTAGE * w6_desc_bytes(); }
 
+// Stage layout, in floats, for G slices of an nx x ny plane (P = nx*ny):
+// the z window, then every k/l/m neighbour plane and every velocity / rate
+// plane with its G slices consecutive (z-consecutive planes of one (k,l,m)
+// are consecutive in HBM too, so each group is one bulk copy), then the
+// face-0 rows of the slices.
 struct W6Layout {
   int P, G, nx, ny;
   __host__ __device__ int ez(int zz) const { return zz * P; }   // zz = z - z0 + 2
-  __host__ __device__ int en(int g, int a, int i) const { return (G + 4 + g * 12 + (a - 3) * 4 + i) * P; }
-  // v: 0 x, 1 y, 2..5 right faces of z..m, 6..9 left faces of z..m, 10 rate
-  __host__ __device__ int v(int g, int k) const { return (G + 4 + 12 * G + g * 11 + k) * P; }
-  __host__ __device__ int b0x(int g) const { return (24 * G + 4) * P + g * (nx + ny); }
-  __host__ __device__ int b0y(int g) const { return b0x(g) + ny; }
+  __host__ __device__ int en(int g, int a, int i) const { return (G + 4 + ((a - 3) * 4 + i) * G + g) * P; }
+  // k: 0 x, 1 y, 2..5 right faces of z..m, 6..9 left faces of z..m, 10 rate
+  __host__ __device__ int v(int g, int k) const { return (G + 4 + 12 * G + k * G + g) * P; }
+  __host__ __device__ int b0x(int g) const { return (24 * G + 4) * P + g * ny; }
+  __host__ __device__ int b0y(int g) const { return (24 * G + 4) * P + G * ny + g * nx; }
   __host__ __device__ int floats() const { return (24 * G + 4) * P + G * (nx + ny); }
-  // z window G+4, k,l,m neighbours 12G, velocities and rate 11G, face-0 rows 2G
-  __host__ __device__ int copies() const { return 26 * G + 4; }
 };
 
 __host__ __device__ __forceinline__ W6Layout w6_layout(const Dims& d, int G) {
   return W6Layout{d.n[0] * d.n[1], G, d.n[0], d.n[1]};
 }
 
-// copy j of an item: what it holds and where it lands in the stage
+// Copy j (0..30) of the item whose first slice is z0: what it holds and
+// where it lands.  Only the live slices (z < nz) are copied; slots of dead
+// slices keep stale data and their results are not stored.
+//   0      E of the z window inside [0, nz) (one range)
+//   1..4   E at z0-2, z0-1, nz, nz+1 when in the window and outside [0, nz)
+//          (boundary-mapped planes)
+//   5..16  k,l,m neighbours (a, i) of all live slices
+//   17..27 velocity / rate planes k = j-17 of all live slices (k = 6, the
+//          left z faces: slices z >= 1 only when z0 == 0)
+//   28     left z faces of slice 0 when z0 == 0 (the face-0 plane of z)
+//   29, 30 face-0 x rows and y rows of the live slices
+#define RT_W6_NCOPY 31
 struct W6Copy {
-  int kind;        // 0 z window, 1 k/l/m neighbour, 2 velocity or rate, 3 face-0 row
-  int g, a, i;     // slice; axis or plane index; offset index / row (0 x, 1 y)
+  bool valid;
+  int kind;        // 0 z range, 1 mapped z plane, 2 neighbour, 3 velocity / rate, 4 face-0 z plane, 5 face-0 rows
+  int a, i, k;     // neighbour axis and offset index; velocity plane; absolute z (kind 0: first z, 1: z)
   int dst;         // stage offset, floats
   unsigned bytes;
 };
-__host__ __device__ __forceinline__ W6Copy w6_copy(const W6Layout& L, int j) {
-  W6Copy c{0, 0, 0, 0, 0, (unsigned)(L.P * sizeof(float))};
+__host__ __device__ __forceinline__ W6Copy w6_copy(const W6Layout& L, int j, int z0, int nz) {
   const int G = L.G;
-  if (j < G + 4) {
+  const int gl = z0 + G < nz ? G : nz - z0;   // live slices
+  const unsigned pb = (unsigned)(L.P * sizeof(float));
+  W6Copy c{false, 0, 0, 0, 0, 0, 0u};
+  if (j == 0) {
+    const int zs = z0 - 2 > 0 ? z0 - 2 : 0, ze = z0 + G + 2 < nz ? z0 + G + 2 : nz;
+    c.valid = ze > zs;
     c.kind = 0;
-    c.i = j;
-    c.dst = L.ez(j);
-    return c;
-  }
-  int jj = j - (G + 4);
-  if (jj < 12 * G) {
+    c.k = zs;
+    c.dst = L.ez(zs - z0 + 2);
+    c.bytes = (unsigned)(ze - zs) * pb;
+  } else if (j <= 4) {
+    const int za = j == 1 ? z0 - 2 : (j == 2 ? z0 - 1 : (j == 3 ? nz : nz + 1));
+    c.valid = (za < 0 || za >= nz) && za >= z0 - 2 && za < z0 + G + 2;
     c.kind = 1;
-    c.g = jj / 12;
-    c.a = 3 + (jj % 12) / 4;
-    c.i = jj % 4;
-    c.dst = L.en(c.g, c.a, c.i);
-    return c;
-  }
-  jj -= 12 * G;
-  if (jj < 11 * G) {
+    c.k = za;
+    c.dst = L.ez(za - z0 + 2);
+    c.bytes = pb;
+  } else if (j <= 16) {
+    c.valid = true;
     c.kind = 2;
-    c.g = jj / 11;
-    c.a = jj % 11;
-    c.dst = L.v(c.g, c.a);
-    return c;
+    c.a = 3 + (j - 5) / 4;
+    c.i = (j - 5) % 4;
+    c.dst = L.en(0, c.a, c.i);
+    c.bytes = (unsigned)gl * pb;
+  } else if (j <= 27) {
+    c.kind = 3;
+    c.k = j - 17;
+    const int first = (c.k == 6 && z0 == 0) ? 1 : 0;
+    c.valid = gl > first;
+    c.dst = L.v(first, c.k);
+    c.bytes = (unsigned)(gl - first) * pb;
+  } else if (j == 28) {
+    c.valid = z0 == 0;
+    c.kind = 4;
+    c.dst = L.v(0, 6);
+    c.bytes = pb;
+  } else if (j <= 30) {
+    c.valid = true;
+    c.kind = 5;
+    c.i = j - 29;
+    c.dst = c.i == 0 ? L.b0x(0) : L.b0y(0);
+    c.bytes = (unsigned)(gl * (c.i == 0 ? L.ny : L.nx)) * (unsigned)sizeof(float);
   }
-  jj -= 11 * G;
-  c.kind = 3;
-  c.g = jj / 2;
-  c.i = jj % 2;
-  c.dst = c.i == 0 ? L.b0x(c.g) : L.b0y(c.g);
-  c.bytes = (unsigned)((c.i == 0 ? L.ny : L.nx) * sizeof(float));
   return c;
 }
-// bytes the item's mbarrier expects: the sum of w6_copy(L, j).bytes
-__host__ __device__ __forceinline__ unsigned w6_tx_bytes(const W6Layout& L) {
-  return (unsigned)((L.G + 4 + 23 * L.G) * L.P * sizeof(float) + L.G * (L.nx + L.ny) * sizeof(float));
+// bytes an item's mbarrier expects: the sum of its valid copies' bytes
+__host__ __device__ __forceinline__ unsigned w6_tx_bytes(const W6Layout& L, int z0, int nz) {
+  unsigned t = 0;
+  for (int j = 0; j < RT_W6_NCOPY; j++) {
+    const W6Copy c = w6_copy(L, j, z0, nz);
+    if (c.valid) t += c.bytes;
+  }
+  return t;
 }
 
 // item -> (z0, k, l, m) for z groups of G slices (band order of rt_step6.cuh)
@@ -125,7 +158,8 @@ __host__ __device__ __forceinline__ long long w6_items(const Dims& d, int G) {
   return (long long)((d.n[2] + G - 1) / G) * d.n[3] * d.n[4] * d.n[5];
 }
 
-// one item into a stage, by the 32 lanes of the producer warp
+// one item into a stage, by the 32 lanes of the producer warp (one copy
+// per lane, w6_copy)
 __device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSched& S, long long li, int member,
                                          float* sP, W6Desc* D, uint64_t* fullb, uint64_t* dfulb) {
   const Dims& d = A.d;
@@ -138,6 +172,7 @@ __device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSc
   const int z0 = c[2];
   const long long p0 = (long long)z0 * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                        (long long)c[5] * d.s[5];
+  const W6Copy cp = w6_copy(L, lane, z0, nz);
   if (lane == 0) {
     D->p0 = p0;
     D->member = member;
@@ -155,53 +190,52 @@ __device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSc
       D->zl[g] = A.t32.hcfl[2][pidx(z)];
     }
     mbar_arrive(dfulb);
-    mbar_arrive_expect_tx(fullb, w6_tx_bytes(L));
+    mbar_arrive_expect_tx(fullb, w6_tx_bytes(L, z0, nz));
   }
   __syncwarp();
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  const int ncopy = L.copies();
-  for (int j = lane; j < ncopy; j += 32) {
-    const W6Copy cp = w6_copy(L, j);
+  if (lane < RT_W6_NCOPY && cp.valid) {
     const float* src;
-    if (cp.kind == 0) {
-      // the shared z window; rows past nz+1 only feed slices past nz
-      int za = z0 - 2 + cp.i;
-      if (za > nz + 1) za = nz + 1;
+    if (cp.kind == 0) {   // z range inside the field: planes (z, k, l, m) are consecutive
+      src = A.E + (p0 + (long long)(cp.k - z0) * d.s[2]);
+    } else if (cp.kind == 1) {   // one boundary-mapped z plane
       int flip = 0;
-      const int zm = map_coord(d, 2, za, flip);
+      const int zm = map_coord(d, 2, cp.k, flip);
       const int m = flip ? d.n[5] - 1 - c[5] : c[5];
       src = A.E + ((long long)zm * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                    (long long)m * d.s[5]);
-    } else {
-      int cg[6] = {0, 0, c[2], c[3], c[4], c[5]};
-      cg[2] = z0 + cp.g < nz ? z0 + cp.g : nz - 1;
-      if (cp.kind == 1) {
-        src = A.E + nb_plane(d, cg, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1);
-      } else if (cp.kind == 2) {
-        const long long pg = p0 + (long long)(cg[2] - z0) * d.s[2];
-        const int k = cp.a;
-        if (k < 6) {
-          src = A.vel[k] + pg;
-        } else if (k < 10) {
-          const int a = k - 4;
-          if (cg[a] > 0) {
-            src = A.vel[a] + (pg - d.s[a]);
-          } else {
-            long long off = 0;
-#pragma unroll
-            for (int b = 2; b < 6; b++) off += (long long)cg[b] * d.ps[a][b];
-            src = A.vlo[a] + off;
-          }
+    } else if (cp.kind == 2) {   // the k/l/m maps do not depend on z: slices consecutive
+      src = A.E + nb_plane(d, c, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1);
+    } else if (cp.kind == 3) {
+      const int k = cp.k;
+      if (k < 6) {
+        src = A.vel[k] + p0;
+      } else if (k < 10) {
+        const int a = k - 4;
+        if (a == 2) {
+          src = A.vel[2] + (z0 > 0 ? p0 - d.s[2] : p0);   // left z faces of slices z >= 1
+        } else if (c[a] > 0) {
+          src = A.vel[a] + (p0 - d.s[a]);
         } else {
-          src = A.lam[0] + pg;
+          long long off = 0;
+#pragma unroll
+          for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+          src = A.vlo[a] + off;
         }
       } else {
-        long long off = 0;   // face-0 x row (by y) or face-0 y row (by x) of the slice
-#pragma unroll
-        for (int b = 2; b < 6; b++) off += (long long)cg[b] * d.ps[cp.i][b];
-        src = A.vlo[cp.i] + off;
+        src = A.lam[0] + p0;
       }
+    } else if (cp.kind == 4) {   // left z faces of slice z = 0: the face-0 plane of z
+      long long off = 0;
+#pragma unroll
+      for (int b = 3; b < 6; b++) off += (long long)c[b] * d.ps[2][b];
+      src = A.vlo[2] + off;
+    } else {   // face-0 x rows (by y) or y rows (by x) of the live slices
+      long long off = 0;
+#pragma unroll
+      for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.i][b];
+      src = A.vlo[cp.i] + off;
     }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     bulk_g2s(sP + cp.dst, src, cp.bytes, fullb);
   }
 }

@@ -200,10 +200,11 @@ class GpuExecutor:
 
     overlap_setup = True   # Server runs admit_async in worker threads
 
-    def __init__(self, precision="fp32", tune=False, batch_tuning=None):
+    def __init__(self, precision="fp32", tune=False, batch_tuning=None, persistent=None):
         self.precision = precision
         self.tune = tune
         self.batch_tuning = batch_tuning
+        self.persistent = persistent     # consumer threads of the staged classes (None: library default)
         self._batch = None
         self._members = None
 
@@ -236,6 +237,8 @@ class GpuExecutor:
             self._batch = Batch(members)
             if self.batch_tuning:
                 self._batch.set_tuning(*self.batch_tuning)
+                if self.persistent is not None:
+                    self._batch.set_persistent(self.persistent)
             elif self.tune:
                 from .autotune import tune_batch
                 tune_batch(self._batch)

@@ -1,10 +1,12 @@
 // Host-side check of the shared-memory stage layouts of the staged binary32
 // kernels (rt_step8.cuh, rt_step11.cuh), compiled from the same headers the
-// kernels use.  For every shape it enumerates an item's bulk copies and
-// checks: the bytes the stage's mbarrier expects equal the bytes copied (a
-// mismatch leaves the barrier incomplete), every copy lands inside the
-// stage, copies do not overlap, and destinations and sizes are multiples of
-// 16 bytes (the bulk-copy rule).  Exit status 0 when every shape passes.
+// kernels use.  For every shape (and, for the z-slice kernel, every first
+// slice of an item) it enumerates an item's bulk copies and checks: the
+// bytes the stage's mbarrier expects equal the bytes copied (a mismatch
+// leaves the barrier incomplete), every copy lands inside the stage, copies
+// do not overlap, destinations and sizes are multiples of 16 bytes (the
+// bulk-copy rule), and every shared-memory slot the consumers read for a
+// live cell is written by a copy.  Exit status 0 when every shape passes.
 #include <cstdio>
 #include <vector>
 #include <algorithm>
@@ -58,6 +60,30 @@ int main() {
                 tot += c.bytes;
                 r.push_back({c.dst * 4, c.dst * 4 + (long long)c.bytes});
               }
+              {
+                const long long pb = (long long)nx * ny * 4;
+                auto covered = [&](long long lo, long long hi) {
+                  for (auto& q : r)
+                    if (q.first <= lo && hi <= q.second) return true;
+                  return false;
+                };
+                bool ok = covered(0, pb) && covered((long long)RT_W3_VX * pb, (RT_W3_VX + 1) * pb) &&
+                          covered((long long)RT_W3_VY * pb, (RT_W3_VY + 1) * pb) &&
+                          covered((long long)RT_W3_LAM * pb, (RT_W3_LAM + 1) * pb) &&
+                          covered((long long)RT_W3_NPL * pb, RT_W3_NPL * pb + ny * 4LL) &&
+                          covered(RT_W3_NPL * pb + ny * 4LL, RT_W3_NPL * pb + (nx + ny) * 4LL);
+                for (int a = 2; a < 6; a++) {
+                  if (d.n[a] < 2) continue;
+                  for (int i = 0; i < 4; i++)
+                    ok = ok && covered((1 + 4 * (a - 2) + i) * pb, (2 + 4 * (a - 2) + i) * pb);
+                  ok = ok && covered((RT_W3_VR + a - 2) * pb, (RT_W3_VR + a - 1) * pb) &&
+                       covered((RT_W3_VL + a - 2) * pb, (RT_W3_VL + a - 1) * pb);
+                }
+                if (!ok) {
+                  std::printf("w3 plane read but not written: n=%d,%d,%d,%d,2,%d\n", nx, ny, nz, nk, nm);
+                  bad++;
+                }
+              }
               if (tot != w3_tx_bytes(d)) {
                 std::printf("w3 expects %u bytes, copies %llu: n=%d,%d,%d,%d,2,%d\n", w3_tx_bytes(d), tot, nx, ny,
                             nz, nk, nm);
@@ -68,26 +94,49 @@ int main() {
             // ---- z-slice kernel (every axis z..m longer than one) ----
             if (nz < 2 || nk < 2 || nm < 2) continue;
             for (int G = 1; G <= RT_W6_MAXG && G <= nz; G++) {
-              w6_shapes++;
               const W6Layout L = w6_layout(d, G);
               const long long limit = (long long)L.floats() * 4;
-              unsigned long long tot = 0;
-              std::vector<std::pair<long long, long long>> r;
-              for (int j = 0; j < L.copies(); j++) {
-                const W6Copy c = w6_copy(L, j);
-                if (((long long)c.dst * 4) % 16 || c.bytes % 16) {
-                  std::printf("w6 copy %d misaligned: n=%d,%d G=%d\n", j, nx, ny, G);
+              for (int z0 = 0; z0 < nz; z0 += G) {
+                w6_shapes++;
+                unsigned long long tot = 0;
+                std::vector<std::pair<long long, long long>> r;
+                for (int j = 0; j < RT_W6_NCOPY; j++) {
+                  const W6Copy c = w6_copy(L, j, z0, nz);
+                  if (!c.valid) continue;
+                  if (((long long)c.dst * 4) % 16 || c.bytes % 16 || c.bytes == 0) {
+                    std::printf("w6 copy %d misaligned or empty: n=%d,%d G=%d z0=%d\n", j, nx, ny, G, z0);
+                    bad++;
+                  }
+                  tot += c.bytes;
+                  r.push_back({(long long)c.dst * 4, (long long)c.dst * 4 + c.bytes});
+                }
+                if (tot != w6_tx_bytes(L, z0, nz)) {
+                  std::printf("w6 expects %u bytes, copies %llu\n", w6_tx_bytes(L, z0, nz), tot);
                   bad++;
                 }
-                tot += c.bytes;
-                r.push_back({(long long)c.dst * 4, (long long)c.dst * 4 + c.bytes});
+                bad += check_ranges(r, limit, "w6", d.n, G);
+                // every slot a live slice reads is written by a copy
+                auto covered = [&](long long lo, long long hi) {
+                  for (auto& q : r)
+                    if (q.first <= lo && hi <= q.second) return true;
+                  return false;
+                };
+                const long long pb = (long long)L.P * 4;
+                for (int g = 0; g < G && z0 + g < nz; g++) {
+                  bool ok = true;
+                  for (int zz = g; zz <= g + 4; zz++) ok = ok && covered((long long)L.ez(zz) * 4, L.ez(zz) * 4 + pb);
+                  for (int a = 3; a < 6; a++)
+                    for (int i = 0; i < 4; i++) ok = ok && covered((long long)L.en(g, a, i) * 4, L.en(g, a, i) * 4 + pb);
+                  for (int k = 0; k < 11; k++) ok = ok && covered((long long)L.v(g, k) * 4, L.v(g, k) * 4 + pb);
+                  ok = ok && covered((long long)L.b0x(g) * 4, (L.b0x(g) + ny) * 4LL);
+                  ok = ok && covered((long long)L.b0y(g) * 4, (L.b0y(g) + nx) * 4LL);
+                  if (!ok) {
+                    std::printf("w6 slot of live slice %d not written: n=%d,%d,%d G=%d z0=%d\n", g, nx, ny, nz, G, z0);
+                    bad++;
+                    break;
+                  }
+                }
               }
-              if (tot != w6_tx_bytes(L)) {
-                std::printf("w6 expects %u bytes, copies %llu: n=%d,%d,%d G=%d\n", w6_tx_bytes(L), tot, nx, ny, nz,
-                            G);
-                bad++;
-              }
-              bad += check_ranges(r, limit, "w6", d.n, G);
             }
           }
   std::printf("stage layouts: %d plane-kernel shapes, %d z-slice shapes, %d failures\n", w3_shapes, w6_shapes, bad);
