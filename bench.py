@@ -244,10 +244,11 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None):
         models.append(m)
     setup_s = time.perf_counter() - t0
     b = Batch(models)
-    if fixed:   # band, threads, sweep, persistent threads (profiling runs)
+    if fixed:   # band, threads, sweep, persistent threads[, slice threads] (profiling runs)
         b.set_tuning(fixed[0], fixed[1], fixed[2], 16)
         b.set_persistent(fixed[3])
-        best = tuple(fixed)
+        b.set_slices(fixed[4] if len(fixed) > 4 else -1)
+        best = tuple(fixed) + ((-1,) if len(fixed) < 5 else ())
     else:
         best, table = tune_batch(b, reps=2, use_cache=False)
     b.integrate(warmup)
@@ -268,7 +269,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None):
            "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": b.launch_count() - l0,
            "graph_steps": b.tuning[3],
            "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
-                      "persistent_members": b.persistent_members()},
+                      "slice_threads": best[4], "staged_members": b.persistent_members()},
            "roofline": roofline("fp32", cells, secs / steps), "clocks": cs.summary(),
            "setup_s": round(setup_s, 2)}
     b.close()
@@ -414,7 +415,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--batch-members", type=int, default=48)
-    ap.add_argument("--batch-tuning", default=None, help="band,threads,sweep,persistent (skip the batch tuner)")
+    ap.add_argument("--batch-tuning", default=None,
+                    help="band,threads,sweep,persistent[,slices] (skip the batch tuner)")
     ap.add_argument("--only", default="all", choices=("all", "batch"), help="batch: the batched form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)
     args = ap.parse_args()

@@ -213,6 +213,9 @@ int rt_batch_set_tuning(rt_batch* b, int band, int threads, int sweep, int graph
  * others by the z-group / plane kernels.  0 puts every member in the last
  * class.  Default 256.  No effect on results. */
 int rt_batch_set_persistent(rt_batch* b, int threads);
+/* consumer threads (256 or 512) of the small-plane class alone; 0 turns
+ * that class off, -1 (default) follows rt_batch_set_persistent */
+int rt_batch_set_slices(rt_batch* b, int threads);
 /* number of members in the two warp-specialised classes (negative: error) */
 int rt_batch_persistent_members(rt_batch* b);
 /* advance every member by nsteps (asynchronous on the batch stream) */

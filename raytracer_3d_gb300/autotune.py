@@ -97,9 +97,9 @@ def tune_model(model, candidates=None, reps=3, use_cache=True):
 
 
 BATCH_CANDIDATES = [
-    (band, threads, sweep, persistent)
+    (band, 512, sweep, persistent, slices)
     for persistent in (256, 512, 0)
-    for threads in (256, 512, 1024)
+    for slices in (256, 512, 0)
     for band in (4, 8)
     for sweep in (0, 1)
 ]
@@ -107,28 +107,31 @@ BATCH_CANDIDATES = [
 
 def tune_batch(batch, candidates=None, reps=2, graph_steps=16, use_cache=True):
     """Pick band / CTA size / sweep order of the plane and group kernels and
-    the consumer threads of the warp-specialised class (0: off) for a Batch;
-    returns (best, table) with best = (band, threads, sweep, persistent)."""
-    key = signature("batch2", sorted(m.n for m in batch.models), batch.models[0].precision)
+    the consumer threads of the two staged classes (0: off) for a Batch;
+    returns (best, table) with best = (band, threads, sweep, persistent,
+    slices)."""
+    key = signature("batch3", sorted(m.n for m in batch.models), batch.models[0].precision)
     cache = _load_cache() if use_cache else {}
+
+    def apply(c):
+        batch.set_tuning(c[0], c[1], c[2], graph_steps)
+        batch.set_persistent(c[3])
+        batch.set_slices(c[4])
+
     if use_cache and key in cache:
-        band, threads, sweep, persistent = cache[key]["best"]
-        batch.set_tuning(band, threads, sweep, graph_steps)
-        batch.set_persistent(persistent)
+        apply(cache[key]["best"])
         return tuple(cache[key]["best"]), cache[key].get("table", [])
     lib = batch._lib
     timed = _event_timer(batch.stream())
     table = []
-    for band, threads, sweep, persistent in candidates or BATCH_CANDIDATES:
-        batch.set_tuning(band, threads, sweep, graph_steps)
-        batch.set_persistent(persistent)
+    for cand in candidates or BATCH_CANDIDATES:
+        apply(cand)
         run = lambda k: batch._check(lib.rt_batch_dry(batch._b, k), "rt_batch_dry")  # noqa: E731
         run(1)
-        table.append(((band, threads, sweep, persistent), timed(run, reps)))
+        table.append((tuple(cand), timed(run, reps)))
     table.sort(key=lambda x: x[1])
     best = table[0][0]
-    batch.set_tuning(best[0], best[1], best[2], graph_steps)
-    batch.set_persistent(best[3])
+    apply(best)
     if use_cache:
         cache[key] = {"best": list(best), "table": [[list(c), t] for c, t in table], "when": time.time()}
         _store_cache(cache)

@@ -41,6 +41,11 @@ class Batch:
         self._check(self._lib.rt_batch_set_persistent(self._b, int(threads)), "rt_batch_set_persistent")
         self.persistent = int(threads)
 
+    def set_slices(self, threads=-1):
+        """consumer threads of the small-plane class (0: off, -1: as set_persistent)"""
+        self._check(self._lib.rt_batch_set_slices(self._b, int(threads)), "rt_batch_set_slices")
+        self.slices = int(threads)
+
     def persistent_members(self):
         n = self._lib.rt_batch_persistent_members(self._b)
         if n < 0:

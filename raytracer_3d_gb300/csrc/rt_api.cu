@@ -274,6 +274,7 @@ struct rt_batch {
   long long* d_sfirst = nullptr;
   int sns = 0, sgrid = 0, sthreads = 0;
   long long sstage = 0;
+  int slice_threads = -1;       // consumer threads of the z-slice class; -1: as pthreads, 0: off
 };
 
 static int bfail(rt_batch* b, int code, const char* fmt, ...) {
@@ -387,8 +388,9 @@ template <class T>
 static int batch_build_slices(rt_batch* b, std::vector<int>& rest) {
   const int n = (int)b->mem.size();
   b->ns6 = 0;
-  if (sizeof(T) != 4 || b->pthreads <= 0) return RT_OK;
-  const int nt = b->pthreads >= 256 ? b->pthreads : 256;
+  const int want = b->slice_threads >= 0 ? b->slice_threads : b->pthreads;
+  if (sizeof(T) != 4 || want <= 0) return RT_OK;
+  const int nt = want >= 256 ? want : 256;
   std::vector<int> sm, left;
   std::vector<int> G;
   long long stage = 0;
@@ -637,6 +639,16 @@ int rt_batch_set_persistent(rt_batch* b, int threads) {
     return bfail(b, RT_ERR_ARG, "rt_batch_set_persistent: threads must be 0, 128, 256 or 512");
   cudaStreamSynchronize(b->st);
   b->pthreads = threads;
+  b->dirty = true;
+  return RT_OK;
+}
+
+int rt_batch_set_slices(rt_batch* b, int threads) {
+  if (!b) return RT_ERR_ARG;
+  if (threads != -1 && threads != 0 && threads != 256 && threads != 512)
+    return bfail(b, RT_ERR_ARG, "rt_batch_set_slices: threads must be -1, 0, 256 or 512");
+  cudaStreamSynchronize(b->st);
+  b->slice_threads = threads;
   b->dirty = true;
   return RT_OK;
 }

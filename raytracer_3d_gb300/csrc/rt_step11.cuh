@@ -158,10 +158,21 @@ __host__ __device__ __forceinline__ long long w6_items(const Dims& d, int G) {
   return (long long)((d.n[2] + G - 1) / G) * d.n[3] * d.n[4] * d.n[5];
 }
 
-// one item into a stage, by the 32 lanes of the producer warp (one copy
-// per lane, w6_copy)
-__device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSched& S, long long li, int member,
-                                         float* sP, W6Desc* D, uint64_t* fullb, uint64_t* dfulb) {
+// One item into a stage, by the 32 lanes of the producer warp, split as in
+// rt_step8.cuh: w6_prepare (before the stage is free) decodes the item, works
+// out each lane's copy (w6_copy) and loads the descriptor's constants,
+// lane-distributed (lane g < G: the z faces of slice g; lanes 16..18: axes
+// k, l, m); w6_commit writes the descriptor, arms the stage and issues the
+// copies.
+struct W6Prep {
+  long long p0;
+  int z0;
+  const float* src;   // null: no copy on this lane
+  int dst;
+  unsigned bytes, tx;
+  float c0, c1, c2;   // this lane's descriptor constants
+};
+__device__ __forceinline__ W6Prep w6_prepare(const StepArgs<float>& A, const PlaneSched& S, long long li) {
   const Dims& d = A.d;
   const int lane = threadIdx.x & 31;
   const int G = S.gz;
@@ -172,71 +183,98 @@ __device__ __forceinline__ void w6_issue(const StepArgs<float>& A, const PlaneSc
   const int z0 = c[2];
   const long long p0 = (long long)z0 * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                        (long long)c[5] * d.s[5];
-  const W6Copy cp = w6_copy(L, lane, z0, nz);
-  if (lane == 0) {
-    D->p0 = p0;
-    D->member = member;
-    D->z0 = z0;
-#pragma unroll
-    for (int a = 3; a < 6; a++) {
-      D->kr[a - 2] = A.t32.hcfl[a][pidx(c[a] + 1)];
-      D->ki[a - 2] = A.t32.inv_d[a][pidx(c[a] + 1)];
-      D->kl[a - 2] = A.t32.hcfl[a][pidx(c[a])];
-    }
-    for (int g = 0; g < G; g++) {
-      const int z = z0 + g < nz ? z0 + g : nz - 1;
-      D->zr[g] = A.t32.hcfl[2][pidx(z + 1)];
-      D->zi[g] = A.t32.inv_d[2][pidx(z + 1)];
-      D->zl[g] = A.t32.hcfl[2][pidx(z)];
-    }
-    mbar_arrive(dfulb);
-    mbar_arrive_expect_tx(fullb, w6_tx_bytes(L, z0, nz));
+  W6Prep P;
+  P.p0 = p0;
+  P.z0 = z0;
+  P.c0 = P.c1 = P.c2 = 0.f;
+  if (lane < G) {
+    const int z = z0 + lane < nz ? z0 + lane : nz - 1;
+    P.c0 = A.t32.hcfl[2][pidx(z + 1)];
+    P.c1 = A.t32.inv_d[2][pidx(z + 1)];
+    P.c2 = A.t32.hcfl[2][pidx(z)];
+  } else if (lane >= 16 && lane < 19) {
+    const int a = lane - 13;
+    P.c0 = A.t32.hcfl[a][pidx(c[a] + 1)];
+    P.c1 = A.t32.inv_d[a][pidx(c[a] + 1)];
+    P.c2 = A.t32.hcfl[a][pidx(c[a])];
   }
-  __syncwarp();
+  const W6Copy cp = w6_copy(L, lane, z0, nz);
+  P.dst = cp.dst;
+  P.bytes = cp.bytes;
+  // the item's bytes (= w6_tx_bytes), summed across the lanes' own copies
+  P.tx = __reduce_add_sync(0xffffffffu, (lane < RT_W6_NCOPY && cp.valid) ? cp.bytes : 0u);
+  P.src = nullptr;
   if (lane < RT_W6_NCOPY && cp.valid) {
-    const float* src;
     if (cp.kind == 0) {   // z range inside the field: planes (z, k, l, m) are consecutive
-      src = A.E + (p0 + (long long)(cp.k - z0) * d.s[2]);
+      P.src = A.E + (p0 + (long long)(cp.k - z0) * d.s[2]);
     } else if (cp.kind == 1) {   // one boundary-mapped z plane
       int flip = 0;
       const int zm = map_coord(d, 2, cp.k, flip);
       const int m = flip ? d.n[5] - 1 - c[5] : c[5];
-      src = A.E + ((long long)zm * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
-                   (long long)m * d.s[5]);
+      P.src = A.E + ((long long)zm * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+                     (long long)m * d.s[5]);
     } else if (cp.kind == 2) {   // the k/l/m maps do not depend on z: slices consecutive
-      src = A.E + nb_plane(d, c, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1);
+      P.src = A.E + nb_plane(d, c, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1);
     } else if (cp.kind == 3) {
       const int k = cp.k;
       if (k < 6) {
-        src = A.vel[k] + p0;
+        P.src = A.vel[k] + p0;
       } else if (k < 10) {
         const int a = k - 4;
         if (a == 2) {
-          src = A.vel[2] + (z0 > 0 ? p0 - d.s[2] : p0);   // left z faces of slices z >= 1
+          P.src = A.vel[2] + (z0 > 0 ? p0 - d.s[2] : p0);   // left z faces of slices z >= 1
         } else if (c[a] > 0) {
-          src = A.vel[a] + (p0 - d.s[a]);
+          P.src = A.vel[a] + (p0 - d.s[a]);
         } else {
           long long off = 0;
 #pragma unroll
           for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-          src = A.vlo[a] + off;
+          P.src = A.vlo[a] + off;
         }
       } else {
-        src = A.lam[0] + p0;
+        P.src = A.lam[0] + p0;
       }
     } else if (cp.kind == 4) {   // left z faces of slice z = 0: the face-0 plane of z
       long long off = 0;
 #pragma unroll
       for (int b = 3; b < 6; b++) off += (long long)c[b] * d.ps[2][b];
-      src = A.vlo[2] + off;
+      P.src = A.vlo[2] + off;
     } else {   // face-0 x rows (by y) or y rows (by x) of the live slices
       long long off = 0;
 #pragma unroll
       for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.i][b];
-      src = A.vlo[cp.i] + off;
+      P.src = A.vlo[cp.i] + off;
     }
+  }
+  return P;
+}
+
+__device__ __forceinline__ void w6_commit(const W6Prep& P, int G, int member, float* sP, W6Desc* D,
+                                          uint64_t* fullb, uint64_t* dfulb) {
+  const int lane = threadIdx.x & 31;
+  if (lane < G) {
+    D->zr[lane] = P.c0;
+    D->zi[lane] = P.c1;
+    D->zl[lane] = P.c2;
+  } else if (lane >= 16 && lane < 19) {
+    D->kr[lane - 15] = P.c0;   // axis a = lane - 13 at index a - 2
+    D->ki[lane - 15] = P.c1;
+    D->kl[lane - 15] = P.c2;
+  }
+  if (lane == 0) {
+    D->p0 = P.p0;
+    D->member = member;
+    D->z0 = P.z0;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    mbar_arrive(dfulb);
+    mbar_arrive_expect_tx(fullb, P.tx);
+  }
+  __syncwarp();
+  if (P.src) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    bulk_g2s(sP + cp.dst, src, cp.bytes, fullb);
+    bulk_g2s(sP + P.dst, P.src, P.bytes, fullb);
   }
 }
 
@@ -389,14 +427,13 @@ __global__ void __launch_bounds__(NT + 32, 1)
     uint32_t rnd = 0;
     long long issued = 0;
     for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
-      if (mem) {
+      if (mem)
         while (it >= first[j + 1]) j++;
-        w6_issue(mem[j].A, mem[j].S, it - first[j], j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s],
-                 &dful[s]);
-      } else {
-        w6_issue(A, S, it, 0, stage0 + (size_t)s * stage_floats, &desc[s], &full[s], &dful[s]);
-      }
+      const StepArgs<float>& Aj = mem ? mem[j].A : A;
+      const PlaneSched& Sj = mem ? mem[j].S : S;
+      const W6Prep P = w6_prepare(Aj, Sj, mem ? it - first[j] : it);
+      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
+      w6_commit(P, Sj.gz, j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s], &dful[s]);
       issued++;
       if (++s == ns) { s = 0; rnd++; }
     }

@@ -94,9 +94,11 @@ __device__ __forceinline__ void ws_decode(const Dims& d, const PlaneSched& S, un
   c[5] = S.sweep ? (int)outer : banded;
 }
 
-// producer: the 32 lanes of the last warp.  All lanes decode the item;
-// lane 0 publishes the descriptor and arms the stage; lane j < 17 issues the
-// bulk copy of plane j (0 = centre, 1 + 4(a-2) + i = neighbour i of axis a).
+// producer: the 32 lanes of the last warp.  All lanes decode the next item
+// and work out their part while the stage is still in use; once it is free,
+// lanes 0 and 2..5 write the descriptor, lane 0 arms the stage, and lane
+// j < 17 issues the bulk copy of plane j (0 = centre, 1 + 4(a-2) + i =
+// neighbour i of axis a).
 __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
                                            int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
                                            WsDesc* desc, float* stage0) {
@@ -111,54 +113,72 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
   uint32_t rnd = 0;   // completed passes over the ring
   long long issued = 0;
   for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-    // stage s is free once every consumer thread released its previous item
-    if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+    // ---- before the stage is free: decode, the lane's copy and its share
+    // of the descriptor (lanes 2..5: axis `lane`; lane 0: offsets) ----
     int c[6];
     ws_decode(d, S, (unsigned)it, c);
     const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                          (long long)c[5] * d.s[5];
+    const float* vlp = nullptr;
+    float kr = 0.f, ki = 0.f, kl = 0.f;
+    if (lane >= 2 && lane < 6) {
+      const int a = lane;
+      if (c[a] > 0) {
+        vlp = A.vel[a] + (p0 - d.s[a]);
+      } else {
+        long long off = 0;
+#pragma unroll
+        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+        vlp = A.vlo[a] + off;
+      }
+      if (d.n[a] > 1) {
+        kr = A.t32.hcfl[a][pidx(c[a] + 1)];
+        ki = A.t32.inv_d[a][pidx(c[a] + 1)];
+        kl = A.t32.hcfl[a][pidx(c[a])];
+      }
+    }
+    long long o0 = 0, o1 = 0;
     if (lane == 0) {
-      WsDesc& D = desc[s];
-      D.p0 = p0;
-      long long o0 = 0, o1 = 0;
 #pragma unroll
       for (int b = 2; b < 6; b++) {
         o0 += (long long)c[b] * d.ps[0][b];
         o1 += (long long)c[b] * d.ps[1][b];
       }
-      D.b0x = A.vlo[0] + o0;
-      D.b0y = A.vlo[1] + o1;
-#pragma unroll
-      for (int a = 2; a < 6; a++) {
-        if (c[a] > 0) {
-          D.vl[a - 2] = A.vel[a] + (p0 - d.s[a]);
-        } else {
-          long long off = 0;
-#pragma unroll
-          for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
-          D.vl[a - 2] = A.vlo[a] + off;
-        }
-        const bool act = d.n[a] > 1;
-        D.kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
-        D.kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
-        D.kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
-      }
-      mbar_arrive(&dful[s]);   // release: the descriptor is visible to waiters
-      mbar_arrive_expect_tx(&full[s], nplanes * pbytes);
     }
-    __syncwarp();
+    const float* src = nullptr;
     if (lane < RT_NPLANE) {
-      bool go = true;
       long long off = p0;
+      bool go = true;
       if (lane > 0) {
         const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
         go = d.n[a] > 1;
         if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
       }
-      if (go) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        bulk_g2s(stage0 + (size_t)s * RT_NPLANE * nxy + (size_t)lane * nxy, A.E + off, pbytes, &full[s]);
-      }
+      if (go) src = A.E + off;
+    }
+    // ---- stage s is free once every consumer thread released its previous item ----
+    if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
+    WsDesc& D = desc[s];
+    if (lane >= 2 && lane < 6) {
+      D.vl[lane - 2] = vlp;
+      D.kcfl_r[lane - 2] = kr;
+      D.kinv_r[lane - 2] = ki;
+      D.kcfl_l[lane - 2] = kl;
+    }
+    if (lane == 0) {
+      D.p0 = p0;
+      D.b0x = A.vlo[0] + o0;
+      D.b0y = A.vlo[1] + o1;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&dful[s]);   // release: the descriptor (ordered by the __syncwarp) is visible to waiters
+      mbar_arrive_expect_tx(&full[s], nplanes * pbytes);
+    }
+    __syncwarp();
+    if (src) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_g2s(stage0 + (size_t)s * RT_NPLANE * nxy + (size_t)lane * nxy, src, pbytes, &full[s]);
     }
     issued++;
     if (++s == ns) { s = 0; rnd++; }

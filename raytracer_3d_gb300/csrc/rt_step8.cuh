@@ -33,7 +33,10 @@ __host__ __device__ __forceinline__ size_t w3_smem(const Dims& d, int ns) {
   return ws_head_bytes() + (size_t)ns * w3_stage_floats(d) * sizeof(float);
 }
 
-// copy `lane` of an item (0..29): what it holds and where it lands
+// copy `lane` of an item (0..29): what it holds and where it lands.  This
+// is the lane map w3_prepare writes out inline; tests/native checks it (bytes
+// against w3_tx_bytes, bounds, overlap, alignment, coverage of every plane
+// the consumers read).
 struct W3Copy {
   bool valid;      // false: the axis is collapsed (no copy)
   int kind;        // 0 E plane, 1 right-face velocities, 2 left-face velocities, 3 x/y velocity or rate, 4 face-0 row
@@ -84,60 +87,106 @@ __host__ __device__ __forceinline__ unsigned w3_tx_bytes(const Dims& d) {
   return (1 + 6 * nact + 3) * pbytes + (unsigned)((d.n[0] + d.n[1]) * sizeof(float));
 }
 
-// One item into stage s, by the 32 lanes of a warp: all lanes decode it,
-// lane 0 publishes the descriptor and arms the stage, lane j issues copy j:
-// 0..16 the E planes (as rt_step6.cuh), 17..20 right and 21..24 left face
-// velocities of z..m, 25 x and 26 y velocities, 27 the rate, 28 and 29 the
-// face-0 rows.  `li` is the item's index within its field, `member` is
-// recorded in the descriptor for the batched form.
-__device__ __forceinline__ void w3_issue(const StepArgs<float>& A, const PlaneSched& S, long long li, int member,
-                                         float* sP, WsDesc* D, uint64_t* fullb, uint64_t* dfulb) {
+// One item into a stage, by the 32 lanes of the producer warp, in two
+// parts.  w3_prepare does everything that does not touch the stage: all
+// lanes decode the item, lane j works out copy j (the lane map of w3_copy:
+// 0..16 the E planes, 17..20 right and 21..24 left face velocities of z..m,
+// 25 x and 26 y velocities, 27 the rate, 28 and 29 the face-0 rows) and
+// lanes 2..5 load the grid constants of axis `lane`.  The producer runs it
+// while the stage is still in use; once the stage is free, w3_commit
+// publishes the descriptor, arms the stage's mbarrier and issues the copies
+// (the ring has only two stages for 32x32 planes, so the producer's latency
+// after the wait shows in the step time).
+struct W3Prep {
+  long long p0;
+  const float* src;   // null: no copy on this lane
+  float* dst;
+  uint32_t bytes;
+  float kr, ki, kl;   // lanes 2..5: constants of axis `lane`
+};
+__device__ __forceinline__ W3Prep w3_prepare(const StepArgs<float>& A, const PlaneSched& S, long long li,
+                                             float* sP) {
   const Dims& d = A.d;
   const int lane = threadIdx.x & 31;
   int c[6];
   ws_decode(d, S, (unsigned)li, c);
-  const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
-                       (long long)c[5] * d.s[5];
-  if (lane == 0) {
-    D->p0 = p0;
-    D->member = member;
-#pragma unroll
-    for (int a = 2; a < 6; a++) {
-      const bool act = d.n[a] > 1;
-      D->kcfl_r[a - 2] = act ? A.t32.hcfl[a][pidx(c[a] + 1)] : 0.f;
-      D->kinv_r[a - 2] = act ? A.t32.inv_d[a][pidx(c[a] + 1)] : 0.f;
-      D->kcfl_l[a - 2] = act ? A.t32.hcfl[a][pidx(c[a])] : 0.f;
-    }
-    mbar_arrive(dfulb);
-    mbar_arrive_expect_tx(fullb, w3_tx_bytes(d));
+  W3Prep P;
+  P.p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
+         (long long)c[5] * d.s[5];
+  const long long p0 = P.p0;
+  P.kr = P.ki = P.kl = 0.f;
+  if (lane >= 2 && lane < 6 && d.n[lane] > 1) {
+    P.kr = A.t32.hcfl[lane][pidx(c[lane] + 1)];
+    P.ki = A.t32.inv_d[lane][pidx(c[lane] + 1)];
+    P.kl = A.t32.hcfl[lane][pidx(c[lane])];
   }
-  __syncwarp();
-  const W3Copy cp = w3_copy(d, lane);
-  if (lane < 30 && cp.valid) {
-    const float* src;
-    if (cp.kind == 0) {
-      src = A.E + (lane == 0 ? p0 : nb_plane(d, c, cp.a, cp.i < 2 ? cp.i - 2 : cp.i - 1));
-    } else if (cp.kind == 1) {
-      src = A.vel[cp.a] + p0;
-    } else if (cp.kind == 2) {
-      if (c[cp.a] > 0) {
-        src = A.vel[cp.a] + (p0 - d.s[cp.a]);
+  const int nx = d.n[0], ny = d.n[1];
+  const long long nxy = (long long)nx * ny;
+  P.src = nullptr;
+  P.dst = nullptr;
+  P.bytes = (uint32_t)(nxy * sizeof(float));
+  if (lane < RT_NPLANE) {
+    long long off = p0;
+    bool go = true;
+    if (lane > 0) {
+      const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
+      go = d.n[a] > 1;
+      if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
+    }
+    if (go) { P.src = A.E + off; P.dst = sP + lane * nxy; }
+  } else if (lane < 25) {
+    const bool right = lane < 21;
+    const int a = 2 + (right ? lane - 17 : lane - 21);
+    if (d.n[a] > 1) {
+      if (right) {
+        P.src = A.vel[a] + p0;
+      } else if (c[a] > 0) {
+        P.src = A.vel[a] + (p0 - d.s[a]);
       } else {
         long long off = 0;
 #pragma unroll
-        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.a][b];
-        src = A.vlo[cp.a] + off;
+        for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+        P.src = A.vlo[a] + off;
       }
-    } else if (cp.kind == 3) {
-      src = (cp.i == 0 ? A.vel[0] : (cp.i == 1 ? A.vel[1] : A.lam[0])) + p0;
-    } else {
-      long long off = 0;   // face-0 x row (by y), face-0 y row (by x)
-#pragma unroll
-      for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[cp.i][b];
-      src = A.vlo[cp.i] + off;
+      P.dst = sP + ((right ? RT_W3_VR : RT_W3_VL) + a - 2) * nxy;
     }
+  } else if (lane < 28) {
+    const int which = lane - 25;   // x velocity, y velocity, rate
+    P.src = (which == 0 ? A.vel[0] : (which == 1 ? A.vel[1] : A.lam[0])) + p0;
+    P.dst = sP + (which == 0 ? RT_W3_VX : (which == 1 ? RT_W3_VY : RT_W3_LAM)) * nxy;
+  } else if (lane < 30) {
+    long long off = 0;
+    const int a = lane - 28;   // face-0 x row (by y), face-0 y row (by x)
+#pragma unroll
+    for (int b = 2; b < 6; b++) off += (long long)c[b] * d.ps[a][b];
+    P.src = A.vlo[a] + off;
+    P.dst = sP + RT_W3_NPL * nxy + (a == 0 ? 0 : ny);
+    P.bytes = (uint32_t)((a == 0 ? ny : nx) * sizeof(float));
+  }
+  return P;
+}
+
+__device__ __forceinline__ void w3_commit(const W3Prep& P, const Dims& d, int member, WsDesc* D,
+                                          uint64_t* fullb, uint64_t* dfulb) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= 2 && lane < 6) {
+    D->kcfl_r[lane - 2] = P.kr;
+    D->kinv_r[lane - 2] = P.ki;
+    D->kcfl_l[lane - 2] = P.kl;
+  }
+  if (lane == 0) {
+    D->p0 = P.p0;
+    D->member = member;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    mbar_arrive(dfulb);   // release: lanes 0..5's descriptor writes (ordered by the __syncwarp)
+    mbar_arrive_expect_tx(fullb, w3_tx_bytes(d));
+  }
+  __syncwarp();
+  if (P.src) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    bulk_g2s(sP + cp.dst, src, cp.bytes, fullb);
+    bulk_g2s(P.dst, P.src, P.bytes, fullb);
   }
 }
 
@@ -320,8 +369,9 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
     uint32_t rnd = 0;
     long long issued = 0;
     for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+      const W3Prep P = w3_prepare(A, S, it, stage0 + (size_t)s * sfl);
       if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, A.status)) break;
-      w3_issue(A, S, it, 0, stage0 + (size_t)s * sfl, &desc[s], &full[s], &dful[s]);
+      w3_commit(P, A.d, 0, &desc[s], &full[s], &dful[s]);
       issued++;
       if (++s == ns) { s = 0; rnd++; }
     }
@@ -377,10 +427,10 @@ __global__ void __launch_bounds__(NT + 32, 1)
     uint32_t rnd = 0;
     long long issued = 0;
     for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
       while (it >= first[j + 1]) j++;
-      w3_issue(mem[j].A, mem[j].S, it - first[j], j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s],
-               &dful[s]);
+      const W3Prep P = w3_prepare(mem[j].A, mem[j].S, it - first[j], stage0 + (size_t)s * stage_floats);
+      if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
+      w3_commit(P, mem[j].A.d, j, &desc[s], &full[s], &dful[s]);
       issued++;
       if (++s == ns) { s = 0; rnd++; }
     }
