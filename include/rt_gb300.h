@@ -128,6 +128,15 @@ int rt_step_dry(rt_handle* h, int nsteps);
 /* One integrate on a host array, the literal drop-in for the module-state
  * call: E is uploaded, stepped once and written back (interior). */
 int rt_integrate_host(rt_handle* h, double* E);
+/* How rt_set_state / rt_get_state / rt_integrate_host move the host's
+ * padded array: direct = 1 (default) lets the GPU read and write it in
+ * place through the host's page tables when the device supports pageable
+ * memory access (cudaDevAttrPageableMemoryAccess, e.g. coherent CPU-GPU
+ * systems); direct = 0, or a device without it, gathers the interior on the
+ * host into pinned staging and copies.  Results are identical. */
+int rt_set_host_access(rt_handle* h, int direct);
+/* 1 when the direct path is in use for this handle, 0 otherwise */
+int rt_host_direct(rt_handle* h);
 
 /* Budget part of diagnose (diagnose.f90:46-329), for the step taken last.
  * The 3D outputs are padded host arrays (interior written; NULL skips).

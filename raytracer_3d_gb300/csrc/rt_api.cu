@@ -52,6 +52,8 @@ struct rt_handle {
   double* result = nullptr;     // DIAG_RESULT_NV doubles
   int* status = nullptr;        // device flag raised by a timed-out wait
   void* pinned = nullptr;       // host staging of one interior field
+  int host_direct = 1;          // 1: the GPU reads / writes host arrays itself when the device can
+  int pageable = -1;            // device supports pageable host memory access (-1: not asked yet)
   double rate = 0.0;
   StepTuning tune;
   bool have_grid = false, have_bg = false, have_coeff = false, have_state = false;
@@ -1011,11 +1013,33 @@ int rt_get_field(rt_handle* h, int which, double* out) {
   return RT_OK;
 }
 
+// true when host arrays are moved by the GPU through the host's page tables
+static bool use_host_direct(rt_handle* h) {
+  if (!h->host_direct) return false;
+  if (h->pageable < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    h->pageable = (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v) ? 1 : 0;
+  }
+  return h->pageable == 1;
+}
+
 int rt_set_state(rt_handle* h, const double* E) {
   if (!h || !E) return RT_ERR_ARG;
+  const Dims& d = h->d;
+  if (use_host_direct(h)) {
+    h->cur = 0;
+    cudaError_t e = h->p.precision == RT_FP64 ? launch_host_gather<double>(E, (double*)h->E[0], d, h->st)
+                                              : launch_host_gather<float>(E, (float*)h->E[0], d, h->st);
+    if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "host gather: %s", cudaGetErrorString(e));
+    h->launches += 1;
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    h->have_state = true;
+    h->steps_since_set = 0;
+    return RT_OK;
+  }
   int rc = ensure_pinned(h);
   if (rc) return rc;
-  const Dims& d = h->d;
   if (h->p.precision == RT_FP64) gather_interior<double>(d, E, (double*)h->pinned);
   else gather_interior<float>(d, E, (float*)h->pinned);
   h->cur = 0;
@@ -1029,15 +1053,35 @@ int rt_set_state(rt_handle* h, const double* E) {
 int rt_get_state(rt_handle* h, double* E) {
   if (!h || !E) return RT_ERR_ARG;
   if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_get_state: no state (rt_set_state first)");
+  const Dims& d = h->d;
+  if (use_host_direct(h)) {
+    cudaError_t e = h->p.precision == RT_FP64
+                        ? launch_host_scatter<double>((const double*)h->E[h->cur], E, d, h->st)
+                        : launch_host_scatter<float>((const float*)h->E[h->cur], E, d, h->st);
+    if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "host scatter: %s", cudaGetErrorString(e));
+    h->launches += 1;
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return check_status(h);
+  }
   int rc = ensure_pinned(h);
   if (rc) return rc;
-  const Dims& d = h->d;
   CUDA_TRY(h, cudaMemcpyAsync(h->pinned, h->E[h->cur], (size_t)d.ncell * h->elem, cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(h, cudaStreamSynchronize(h->st));
   if ((rc = check_status(h))) return rc;
   if (h->p.precision == RT_FP64) scatter_interior<double>(d, (const double*)h->pinned, E);
   else scatter_interior<float>(d, (const float*)h->pinned, E);
   return RT_OK;
+}
+
+int rt_set_host_access(rt_handle* h, int direct) {
+  if (!h || (direct != 0 && direct != 1)) return RT_ERR_ARG;
+  h->host_direct = direct;
+  return RT_OK;
+}
+
+int rt_host_direct(rt_handle* h) {
+  if (!h) return RT_ERR_ARG;
+  return use_host_direct(h) ? 1 : 0;
 }
 
 int rt_integrate(rt_handle* h, int nsteps) {

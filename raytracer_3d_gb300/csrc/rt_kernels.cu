@@ -508,6 +508,52 @@ cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf
   return cudaGetLastError();
 }
 
+// ---- padded host array <-> unpadded device field, read / written by the GPU
+// through the host's page tables (devices with pageable memory access) ----
+// A warp moves one x row: row r of the interior is (y, z, k, l, m) in x-fastest
+// order; the host array is padded by RT_ONX on every axis (Fortran order).
+template <bool TO_DEVICE, class T>
+__global__ void host_rows_kernel(const double* __restrict__ hsrc, double* __restrict__ hdst,
+                                 const T* __restrict__ dsrc, T* __restrict__ ddst, Dims d) {
+  long long P[6];
+#pragma unroll
+  for (int a = 0; a < 6; a++) P[a] = d.n[a] + 2 * RT_ONX;
+  const long long rows = d.ncell / d.n[0];
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = warp; r < rows; r += nwarp) {
+    long long q = r;
+    const int j = (int)(q % d.n[1]); q /= d.n[1];
+    const int k = (int)(q % d.n[2]); q /= d.n[2];
+    const int l = (int)(q % d.n[3]); q /= d.n[3];
+    const int n = (int)(q % d.n[4]);
+    const int m = (int)(q / d.n[4]);
+    const long long h0 = RT_ONX + P[0] * ((j + RT_ONX) + P[1] * ((k + RT_ONX) + P[2] *
+                         ((l + RT_ONX) + P[3] * ((n + RT_ONX) + P[4] * (long long)(m + RT_ONX)))));
+    const long long d0 = r * d.n[0];
+    for (int x = lane; x < d.n[0]; x += 32) {
+      if (TO_DEVICE) ddst[d0 + x] = (T)hsrc[h0 + x];
+      else hdst[h0 + x] = (double)dsrc[d0 + x];
+    }
+  }
+}
+
+template <class T>
+cudaError_t launch_host_gather(const double* host, T* dst, const Dims& d, cudaStream_t st) {
+  host_rows_kernel<true, T><<<8 * 152, 256, 0, st>>>(host, nullptr, nullptr, dst, d);
+  return cudaGetLastError();
+}
+template <class T>
+cudaError_t launch_host_scatter(const T* src, double* host, const Dims& d, cudaStream_t st) {
+  host_rows_kernel<false, T><<<8 * 152, 256, 0, st>>>(nullptr, host, src, nullptr, d);
+  return cudaGetLastError();
+}
+template cudaError_t launch_host_gather<double>(const double*, double*, const Dims&, cudaStream_t);
+template cudaError_t launch_host_gather<float>(const double*, float*, const Dims&, cudaStream_t);
+template cudaError_t launch_host_scatter<double>(const double*, double*, const Dims&, cudaStream_t);
+template cudaError_t launch_host_scatter<float>(const float*, double*, const Dims&, cudaStream_t);
+
 cudaError_t launch_to_fp32(const double* src, float* dst, long long n, cudaStream_t st) {
   to_fp32_kernel<<<4 * 152, 256, 0, st>>>(src, dst, n);
   return cudaGetLastError();

@@ -45,6 +45,12 @@ long long max_rate_partials(const Dims& d);
 cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf, double* partial,
                             double* out, cudaStream_t st);
 cudaError_t launch_to_fp32(const double* src, float* dst, long long n, cudaStream_t st);
+// padded host array (pageable, read / written by the GPU directly) <-> the
+// unpadded device field
+template <class T>
+cudaError_t launch_host_gather(const double* host, T* dst, const Dims& d, cudaStream_t st);
+template <class T>
+cudaError_t launch_host_scatter(const T* src, double* host, const Dims& d, cudaStream_t st);
 cudaError_t launch_ucfl(const Dims& d, const Grid& g, double dt, const double* const* vel,
                         const double* const* vlo, double* const* uc, double* const* ucl,
                         cudaStream_t st);

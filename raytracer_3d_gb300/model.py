@@ -132,6 +132,14 @@ class Model:
         self._check(self._lib.rt_set_state(self._h, _lib.dptr(self.E)), "rt_set_state")
         self._state_on_device = True
 
+    def set_host_access(self, direct=True):
+        """direct: the GPU reads / writes the host array in place when the
+        device supports pageable memory access; else pinned staging."""
+        self._check(self._lib.rt_set_host_access(self._h, 1 if direct else 0), "rt_set_host_access")
+
+    def host_direct(self):
+        return bool(self._lib.rt_host_direct(self._h))
+
     def get_state(self):
         """Download the device E into the host array (interior)."""
         self._check(self._lib.rt_get_state(self._h, _lib.dptr(self.E)), "rt_get_state")
