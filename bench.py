@@ -209,7 +209,7 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
     # end to end through the host-array drop-in (rt_integrate_host)
     if e2e_steps > 0:
         m.get_state()
-        m.integrate_host()  # warm-up of the host path (pinned staging)
+        m.integrate_host()  # warm-up of the host path
         torch.cuda.synchronize()
         barrier(dist)
         t0 = time.perf_counter()
@@ -218,7 +218,7 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
         t1 = time.perf_counter()
         e2e_secs = max_over_ranks(dist, t1 - t0)
         out["e2e"] = {"seconds": e2e_secs, "steps": e2e_steps,
-                      "bytes": cells * 8}
+                      "bytes": cells * 8, "host_access": "direct" if m.host_direct() else "staged"}
         out["finite"] = bool(np.isfinite(m.E).all())
     m.close()
     return out
@@ -366,7 +366,8 @@ def gpu_arm(args):
         e = main["e2e"]
         line["e2e"] = {"value": cells * e["steps"] * world / e["seconds"], "unit": UNIT,
                        "h2d_bytes_per_step": e["bytes"], "d2h_bytes_per_step": e["bytes"],
-                       "api": "rt_integrate_host (padded host array in, stepped array out)"}
+                       "api": "rt_integrate_host (padded host array in, stepped array out)",
+                       "host_access": e["host_access"]}
     line["forms"] = forms
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_steps)
