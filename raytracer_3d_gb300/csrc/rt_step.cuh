@@ -51,7 +51,7 @@ __device__ __forceinline__ double flux_fp64u(double v, double uCFL, double Ea, d
 // doubling is exact), and the centred part plus the first diffusive part,
 // 0.5*(v*(Ec+Eb) - |v|*Rj), is the upwind value v*E_up exactly, so
 //   F = v*E_up + |v|*(1/2 - |v|*dt/(2d)) * psi.
-// For Rj == 0 psi = 0 and the diffusive term vanishes as in the reference
+// For Rj == 0 psi = +-0 and the diffusive term vanishes as in the reference
 // (it is multiplied by Rj there).  hcfl = dt/(2 d(f)).
 __device__ __forceinline__ float flux_fp32(float v, float hcfl, float Ea, float Eb, float Ec, float Ed) {
   const float Rjp = Ed - Ec;
@@ -60,11 +60,12 @@ __device__ __forceinline__ float flux_fp32(float v, float hcfl, float Ea, float 
   const bool pos = v > 0.f;
   const float up = pos ? Rjm : Rjp;
   const float Eu = pos ? Eb : Ec;
-  const bool rp = Rj >= 0.f;
+  // s = sign(Rj) applied by flipping the sign bit (one logic op each)
+  const unsigned s = __float_as_uint(Rj) & 0x80000000u;
   const float a = fabsf(Rj);
-  const float t = rp ? up : -up;
+  const float t = __uint_as_float(__float_as_uint(up) ^ s);
   const float ph = fmaxf(0.f, fminf(2.f * fminf(a, t), fmaxf(a, t)));
-  const float psi = rp ? ph : -ph;
+  const float psi = __uint_as_float(__float_as_uint(ph) ^ s);
   const float av = fabsf(v);
   const float h = av * fmaf(-hcfl, av, 0.5f);
   return fmaf(h, psi, v * Eu);
