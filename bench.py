@@ -285,8 +285,10 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
     from raytracer_3d_gb300.serve import GpuExecutor, SequentialExecutor, Server, poisson_requests
     reqs = poisson_requests(nreq, rate=rate, seed=seed)
     ex = GpuExecutor("fp32", batch_tuning=(8, 512, 1, 16), persistent=512)
-    rep = Server(ex, budget_bytes=budget, chunk_max=50).run(reqs)
+    rep = Server(ex, budget_bytes=budget, chunk_max=50, setup_workers=8).run(reqs)
     ex.close()
+    breakdown = {k: round(v, 2) for k, v in ex.times.items()}
+    breakdown["batch_rebuilds"] = ex.rebuilds
     s = rep.summary()
     for r in reqs:
         r.result = None
@@ -297,7 +299,7 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
     return {"requests": nreq, "arrival_rate_per_s": rate, "budget_bytes": budget,
             "p50_s": s["p50_s"], "p99_s": s["p99_s"], "value": s["cell_updates_per_s"], "unit": UNIT,
             "makespan_s": s["makespan_s"], "chunks": s["chunks"], "backlog_max": s["backlog_max"],
-            "peak_bytes": s["peak_bytes"],
+            "peak_bytes": s["peak_bytes"], "seconds_by_activity": breakdown,
             "fp64_one_at_a_time": {"requests": baseline_req, "value": sb["cell_updates_per_s"],
                                    "p50_s": sb["p50_s"], "p99_s": sb["p99_s"]}}
 
@@ -317,6 +319,11 @@ def gpu_arm(args):
     rank, world, local, dist = dist_init(args.gpus)
     n = tuple(int(v) for v in args.dims.split(",")) if args.dims else (args.n,) * 6
     sched = (args.variant, args.band, args.threads, args.sweep)
+    if args.only == "serve":   # the serving form alone
+        out = bench_serving(nreq=args.serve_requests)
+        if rank == 0:
+            print(json.dumps({"profile_only": "serving", **out}), flush=True)
+        return
     if args.only == "batch":   # profiling runs of the batched form only
         out = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,
                             fixed=tuple(int(v) for v in args.batch_tuning.split(",")) if args.batch_tuning else None)
@@ -418,7 +425,8 @@ def main():
     ap.add_argument("--batch-members", type=int, default=48)
     ap.add_argument("--batch-tuning", default=None,
                     help="band,threads,sweep,persistent[,slices] (skip the batch tuner)")
-    ap.add_argument("--only", default="all", choices=("all", "batch"), help="batch: the batched form alone (profiling)")
+    ap.add_argument("--only", default="all", choices=("all", "batch", "serve"),
+                    help="batch / serve: that form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -137,6 +137,13 @@ int rt_integrate_host(rt_handle* h, double* E);
 int rt_set_host_access(rt_handle* h, int direct);
 /* 1 when the direct path is in use for this handle, 0 otherwise */
 int rt_host_direct(rt_handle* h);
+/* The state without ghost cells, exactly as the device stores it:
+ * nx*ny*nz*nk*nl*nm values, x fastest, binary64 for RT_FP64 handles and
+ * binary32 for RT_FP32 handles.  For callers that keep no padded module
+ * array (the ensemble and serving layers); no counterpart in the
+ * reference, whose state is always the padded module array. */
+int rt_set_state_interior(rt_handle* h, const void* E);
+int rt_get_state_interior(rt_handle* h, void* E);
 
 /* Budget part of diagnose (diagnose.f90:46-329), for the step taken last.
  * The 3D outputs are padded host arrays (interior written; NULL skips).

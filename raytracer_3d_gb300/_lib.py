@@ -57,6 +57,8 @@ SIGNATURES = {
     "rt_get_state": (ctypes.c_int, [_P, _D]),
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_set_state_interior": (ctypes.c_int, [_P, _P]),
+    "rt_get_state_interior": (ctypes.c_int, [_P, _P]),
     "rt_host_direct": (ctypes.c_int, [_P]),
     "rt_integrate_host": (ctypes.c_int, [_P, _D]),
     "rt_diagnose": (ctypes.c_int, [_P, ctypes.POINTER(RtBudget)] + [_D] * 8),

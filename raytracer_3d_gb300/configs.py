@@ -48,13 +48,16 @@ class Experiment:
         return int(np.prod(self.n))
 
 
-def build_model(exp, precision="fp64"):
+def build_model(exp, precision="fp64", padded=True):
     """set_parameter .. calc_parameter for one experiment; returns a Model
     with the initial state uploaded and dt fixed (from the CFL number when
-    the experiment gives one)."""
+    the experiment gives one).  padded=False keeps only the interior of the
+    state on the host (the serving layer; experiments whose initial
+    condition goes through _interior)."""
     m = Model(*exp.n, dt=exp.dt if exp.dt else 1.0, f0=exp.f0, sign_of_omega_i=exp.sign_of_omega_i,
               enable_upper_reflection=exp.upper, enable_lower_reflection=exp.lower,
-              precision=precision, k_fixed=exp.fixed[0], l_fixed=exp.fixed[1], m_fixed=exp.fixed[2])
+              precision=precision, k_fixed=exp.fixed[0], l_fixed=exp.fixed[1], m_fixed=exp.fixed[2],
+              padded=padded)
     m.calc_grid(exp.d_interior)
     exp.background(m)
     exp.initial(m, np.random.Generator(np.random.PCG64(exp.seed)))
@@ -71,6 +74,8 @@ def _mesh3(m):
 
 
 def _interior(m):
+    if not getattr(m, "padded", True):
+        return tuple(slice(0, k) for k in m.n)
     return tuple(slice(ONX, ONX + k) for k in m.n)
 
 

@@ -1073,6 +1073,24 @@ int rt_get_state(rt_handle* h, double* E) {
   return RT_OK;
 }
 
+int rt_set_state_interior(rt_handle* h, const void* E) {
+  if (!h || !E) return RT_ERR_ARG;
+  h->cur = 0;
+  CUDA_TRY(h, cudaMemcpyAsync(h->E[0], E, (size_t)h->d.ncell * h->elem, cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  h->have_state = true;
+  h->steps_since_set = 0;
+  return RT_OK;
+}
+
+int rt_get_state_interior(rt_handle* h, void* E) {
+  if (!h || !E) return RT_ERR_ARG;
+  if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_get_state_interior: no state (rt_set_state first)");
+  CUDA_TRY(h, cudaMemcpyAsync(E, h->E[h->cur], (size_t)h->d.ncell * h->elem, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  return check_status(h);
+}
+
 int rt_set_host_access(rt_handle* h, int direct) {
   if (!h || (direct != 0 && direct != 1)) return RT_ERR_ARG;
   h->host_direct = direct;

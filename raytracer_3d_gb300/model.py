@@ -38,7 +38,7 @@ class Model:
 
     def __init__(self, nx, ny, nz, nk, nl, nm, *, dt, f0=1e-4, sign_of_omega_i=1.0,
                  enable_upper_reflection=True, enable_lower_reflection=True,
-                 precision="fp64", k_fixed=0.0, l_fixed=0.0, m_fixed=0.0):
+                 precision="fp64", k_fixed=0.0, l_fixed=0.0, m_fixed=0.0, padded=True):
         self.n = (nx, ny, nz, nk, nl, nm)
         self.dt = float(dt)
         self.f0 = float(f0)
@@ -48,8 +48,11 @@ class Model:
         self.precision = precision
         self.fixed = (float(k_fixed), float(l_fixed), float(m_fixed))
         self.itt = 0
-        # host arrays of allocate_main_module (main_module.f90:131-232)
-        self.E = zeros_padded(self.n)
+        # host arrays of allocate_main_module (main_module.f90:131-232); with
+        # padded=False the host state is the interior only (no ghost cells),
+        # moved by rt_set_state_interior / rt_get_state_interior
+        self.padded = bool(padded)
+        self.E = zeros_padded(self.n) if self.padded else np.zeros(self.n, order="F")
         n3 = self.n[:3]
         self.Nsqr = zeros_padded(n3)
         self.U = zeros_padded(n3)
@@ -129,7 +132,13 @@ class Model:
     # ---- state ----------------------------------------------------------------
     def set_state(self):
         """Upload the host E (interior) to the device."""
-        self._check(self._lib.rt_set_state(self._h, _lib.dptr(self.E)), "rt_set_state")
+        if self.padded:
+            self._check(self._lib.rt_set_state(self._h, _lib.dptr(self.E)), "rt_set_state")
+        else:
+            dt = np.float64 if self.precision == "fp64" else np.float32
+            src = np.asfortranarray(self.E, dtype=dt)
+            self._check(self._lib.rt_set_state_interior(self._h, src.ctypes.data_as(ctypes.c_void_p)),
+                        "rt_set_state_interior")
         self._state_on_device = True
 
     def set_host_access(self, direct=True):
@@ -141,7 +150,14 @@ class Model:
         return bool(self._lib.rt_host_direct(self._h))
 
     def get_state(self):
-        """Download the device E into the host array (interior)."""
+        """Download the device E into the host array (interior).  With
+        padded=False it returns a new interior array in the handle's
+        precision (binary32 for the fp32 form)."""
+        if not self.padded:
+            out = np.empty(self.n, dtype=np.float64 if self.precision == "fp64" else np.float32, order="F")
+            self._check(self._lib.rt_get_state_interior(self._h, out.ctypes.data_as(ctypes.c_void_p)),
+                        "rt_get_state_interior")
+            return out
         self._check(self._lib.rt_get_state(self._h, _lib.dptr(self.E)), "rt_get_state")
         return self.E
 
@@ -155,6 +171,8 @@ class Model:
 
     def integrate_host(self):
         """One integrate on the host array (upload, step, download)."""
+        if not self.padded:
+            raise ValueError("integrate_host needs the padded host array (Model(..., padded=True))")
         self._check(self._lib.rt_integrate_host(self._h, _lib.dptr(self.E)), "rt_integrate_host")
         self._state_on_device = True
         self.itt += 1

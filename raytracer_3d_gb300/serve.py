@@ -207,6 +207,9 @@ class GpuExecutor:
         self.persistent = persistent     # consumer threads of the staged classes (None: library default)
         self._batch = None
         self._members = None
+        # wall seconds spent per activity (set-up runs in worker threads and overlaps)
+        self.times = {"setup": 0.0, "rebuild": 0.0, "step": 0.0, "sync": 0.0, "retire": 0.0}
+        self.rebuilds = 0
 
     def now(self):
         return time.perf_counter()
@@ -222,7 +225,10 @@ class GpuExecutor:
 
     def admit(self, r):
         from .configs import build_model
-        return build_model(r.exp, self.precision)
+        t0 = time.perf_counter()
+        m = build_model(r.exp, self.precision, padded=False)   # no padded host array
+        self.times["setup"] += time.perf_counter() - t0
+        return m
 
     def admit_async(self, r):
         """set-up in a worker thread: numpy work and the library calls
@@ -231,7 +237,9 @@ class GpuExecutor:
 
     def step(self, members, n):
         from .batch import Batch
+        t0 = time.perf_counter()
         if self._members != [id(m) for m in members]:
+            self.rebuilds += 1
             if self._batch is not None:
                 self._batch.close()
             self._batch = Batch(members)
@@ -243,15 +251,23 @@ class GpuExecutor:
                 from .autotune import tune_batch
                 tune_batch(self._batch)
             self._members = [id(m) for m in members]
+        t1 = time.perf_counter()
         self._batch.integrate(n)
+        t2 = time.perf_counter()
+        self.times["rebuild"] += t1 - t0
+        self.times["step"] += t2 - t1
 
     def sync(self):
         if self._batch is not None:
+            t0 = time.perf_counter()
             self._batch.sync()
+            self.times["sync"] += time.perf_counter() - t0
 
     def retire(self, member):
-        E = member.get_state().copy()
+        t0 = time.perf_counter()
+        E = member.get_state()   # interior, in the member's precision
         member.close()
+        self.times["retire"] += time.perf_counter() - t0
         return E
 
     def close(self):

@@ -274,3 +274,23 @@ def test_fp32_budget_residual():
         assert abs(b["residual"]) <= 1e-5 * scale
     finally:
         m.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_interior_state_matches_padded(precision):
+    """a model without the padded host array (interior state in the
+    handle's precision) steps exactly like the padded one"""
+    exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
+    a = configs.build_model(exp, precision)
+    b = configs.build_model(exp, precision, padded=False)
+    try:
+        a.integrate(4)
+        b.integrate(4)
+        ref = a.get_state()[interior(exp.n)]
+        got = b.get_state()
+        assert got.shape == tuple(exp.n)
+        assert got.dtype == (np.float64 if precision == "fp64" else np.float32)
+        assert np.array_equal(got.astype(np.float64), ref)
+    finally:
+        a.close()
+        b.close()
