@@ -176,7 +176,7 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-FP32_CANDIDATES = ([(v, b, t, s) for v in ("w3", "w2d", "w6") for t in (128, 256, 512) for b in (4, 8)
+FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w2d", "w6") for t in (128, 256, 512) for b in (4, 8)
                     for s in (0, 1)]
                    + [(v, b, t, s) for v in ("pipe", "tma") for t in (256, 512, 1024) for b in (4, 8)
                       for s in (0, 1)])
@@ -411,7 +411,7 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
     ap.add_argument("--dims", default=None, help="nx,ny,nz,nk,nl,nm of a profiling case (with --no-fp64)")
-    ap.add_argument("--variant", default="tma", choices=("w6", "w5", "w5h", "w4", "w3", "w2", "w2d", "ws", "wsd", "pipe", "tma", "group", "plane", "cell"))
+    ap.add_argument("--variant", default="tma", choices=("w2z", "w6", "w5", "w5h", "w4", "w3", "w2", "w2d", "ws", "wsd", "pipe", "tma", "group", "plane", "cell"))
     ap.add_argument("--band", type=int, default=8)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--sweep", type=int, default=0)

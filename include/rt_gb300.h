@@ -163,7 +163,9 @@ int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int,
  * uses variant 2), 0 = plane tiled with plain loads, 1 = one thread per
  * cell; band: values per band of the plane schedule (default 8); threads:
  * CTA size 128, 256, 512 or 1024 (default 512; consumer threads of
- * variants 5 and 6: 128, 256 or 512).  Shapes a variant cannot run fall
+ * variants 5 and 6: 128, 256 or 512).  Variants 7-14 are further forms
+ * of the persistent binary32 kernel (raytracer_3d_gb300.model.Model.VARIANTS;
+ * 8 = 2-wide cell blocks, 14 = the same walking whole z columns).  Shapes a variant cannot run fall
  * back to the next one that can.  Chosen by the autotuner
  * (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);

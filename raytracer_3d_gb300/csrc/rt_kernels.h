@@ -73,6 +73,7 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_W5 11
 #define RT_VARIANT_W5H 12
 #define RT_VARIANT_W6 13
+#define RT_VARIANT_W2Z 14
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule

@@ -141,33 +141,34 @@ bool w2_ok(const Dims& d, int threads) {
          ws_stages(d) >= 2;
 }
 
-template <int NT, int R, int PF>
+// ZM = 1: z-march, the count is the number of (k,l,m) columns
+template <int NT, int R, int PF, int ZM>
 cudaError_t launch_w2_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
   const int ns = ws_stages(A.d);
   const size_t sm = ws_smem(A.d, ns);
-  cudaError_t e = set_smem(step_w2_kernel<NT, R, PF>, sm);
+  cudaError_t e = set_smem(step_w2_kernel<NT, R, PF, ZM>, sm);
   if (e != cudaSuccess) return e;
-  const long long nitems = dense_items(A.d);
+  const long long nitems = ZM ? (long long)A.d.n[3] * A.d.n[4] * A.d.n[5] : dense_items(A.d);
   long long grid = 0;
-  e = persistent_grid(step_w2_kernel<NT, R, PF>, NT + 32, sm, nitems, grid);
+  e = persistent_grid(step_w2_kernel<NT, R, PF, ZM>, NT + 32, sm, nitems, grid);
   if (e != cudaSuccess) return e;
-  step_w2_kernel<NT, R, PF><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
+  step_w2_kernel<NT, R, PF, ZM><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
   return cudaGetLastError();
 }
 
-template <int NT, int PF>
+template <int NT, int PF, int ZM>
 cudaError_t launch_w2_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
   const int R = w2_rows(A.d, NT);
-  if (R == 1) return launch_w2_r<NT, 1, PF>(A, S, st);
-  if (R == 2) return launch_w2_r<NT, 2, PF>(A, S, st);
-  return launch_w2_r<NT, 4, PF>(A, S, st);
+  if (R == 1) return launch_w2_r<NT, 1, PF, ZM>(A, S, st);
+  if (R == 2) return launch_w2_r<NT, 2, PF, ZM>(A, S, st);
+  return launch_w2_r<NT, 4, PF, ZM>(A, S, st);
 }
 
-template <int PF>
+template <int PF, int ZM = 0>
 cudaError_t launch_w2_pf(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st) {
-  if (threads == 128) return launch_w2_nt<128, PF>(A, S, st);
-  if (threads == 256) return launch_w2_nt<256, PF>(A, S, st);
-  return launch_w2_nt<512, PF>(A, S, st);
+  if (threads == 128) return launch_w2_nt<128, PF, ZM>(A, S, st);
+  if (threads == 256) return launch_w2_nt<256, PF, ZM>(A, S, st);
+  return launch_w2_nt<512, PF, ZM>(A, S, st);
 }
 
 // ---- all operands staged ----
@@ -455,6 +456,12 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
     if (tn.threads == 128) return launch_w3_nt<128>(A, S, st);
     if (tn.threads == 256) return launch_w3_nt<256>(A, S, st);
     return launch_w3_nt<512>(A, S, st);
+  }
+  if (tn.variant == RT_VARIANT_W2Z && w2_ok(A.d, tn.threads)) {
+    done = true;
+    // columns of z in band order over (k,l,m): units are k alone (gz = nz)
+    const PlaneSched S = make_sched(A.d, tn, A.d.n[2]);
+    return launch_w2_pf<0, 1>(A, S, tn.threads, st);
   }
   if ((tn.variant == RT_VARIANT_W2 || tn.variant == RT_VARIANT_W2D) && w2_ok(A.d, tn.threads)) {
     done = true;

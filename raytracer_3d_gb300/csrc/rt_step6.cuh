@@ -94,11 +94,62 @@ __device__ __forceinline__ void ws_decode(const Dims& d, const PlaneSched& S, un
   c[5] = S.sweep ? (int)outer : banded;
 }
 
+// column -> (k,l,m) in the band order of ws_decode with units = k only
+// (PlaneSched made with gz = nz: nunits = nk); c[2] is left to the caller
+__device__ __forceinline__ void ws_decode_col(const Dims& d, const PlaneSched& S, unsigned col, int c[6]) {
+  const unsigned nb_axis = S.sweep ? d.n[4] : d.n[5];
+  const unsigned no_axis = S.sweep ? d.n[5] : d.n[4];
+  const unsigned nk = (unsigned)d.n[3];
+  const unsigned per_full = nk * no_axis * (unsigned)S.band;
+  const unsigned b = col / per_full;
+  unsigned rem = col - b * per_full;
+  unsigned bsize = S.band;
+  if ((b + 1) * (unsigned)S.band > nb_axis) bsize = nb_axis - b * (unsigned)S.band;
+  const unsigned k = rem % nk;
+  rem /= nk;
+  const unsigned inner = rem % bsize;
+  const unsigned outer = rem / bsize;
+  const int banded = (int)(b * (unsigned)S.band + inner);
+  c[0] = 0;
+  c[1] = 0;
+  c[3] = (int)k;
+  c[4] = S.sweep ? banded : (int)outer;
+  c[5] = S.sweep ? (int)outer : banded;
+}
+
+// A CTA's sequence of work items.  Plain: items b, b+G, b+2G, ... of the
+// band order (count = items).  Z-march: whole z columns -- columns b, b+G,
+// ... of the band order over (k,l,m), each column's planes z = 0..nz-1 in
+// turn (count = columns), so consecutive items of a CTA are z neighbours.
+template <bool ZM>
+struct ItemWalk {
+  long long it;   // item (plain) or column (z-march)
+  int z;          // z-march: plane within the column
+  __device__ __forceinline__ void start() { it = blockIdx.x; z = 0; }
+  __device__ __forceinline__ bool valid(long long count) const { return it < count; }
+  __device__ __forceinline__ void next(int nz) {
+    if (ZM) {
+      if (++z == nz) { z = 0; it += gridDim.x; }
+    } else {
+      it += gridDim.x;
+    }
+  }
+  __device__ __forceinline__ void decode(const Dims& d, const PlaneSched& S, int c[6]) const {
+    if (ZM) {
+      ws_decode_col(d, S, (unsigned)it, c);
+      c[2] = z;
+    } else {
+      ws_decode(d, S, (unsigned)it, c);
+    }
+  }
+};
+
 // producer: the 32 lanes of the last warp.  All lanes decode the next item
 // and work out their part while the stage is still in use; once it is free,
 // lanes 0 and 2..5 write the descriptor, lane 0 arms the stage, and lane
 // j < 17 issues the bulk copy of plane j (0 = centre, 1 + 4(a-2) + i =
 // neighbour i of axis a).
+template <bool ZM = false>
 __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const PlaneSched& S, long long nitems,
                                            int ns, uint64_t* full, uint64_t* empty, uint64_t* dful,
                                            WsDesc* desc, float* stage0) {
@@ -112,11 +163,12 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
   int s = 0;
   uint32_t rnd = 0;   // completed passes over the ring
   long long issued = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+  ItemWalk<ZM> w;
+  for (w.start(); w.valid(nitems); w.next(d.n[2])) {
     // ---- before the stage is free: decode, the lane's copy and its share
     // of the descriptor (lanes 2..5: axis `lane`; lane 0: offsets) ----
     int c[6];
-    ws_decode(d, S, (unsigned)it, c);
+    w.decode(d, S, c);
     const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                          (long long)c[5] * d.s[5];
     const float* vlp = nullptr;

@@ -58,7 +58,11 @@ __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& 
 template <int NT, int R>
 struct W2MinBlocks { static constexpr int value = 1; };
 
-template <int NT, int R, int PF>
+// ZM = 1: z-march (ItemWalk): the CTA walks whole z columns, so the flux a
+// cell computes on its right z face is the next item's left z face flux of
+// the same cell (same inputs: the value is carried, bit-identical).
+// nitems counts columns then.
+template <int NT, int R, int PF, int ZM = 0>
 __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
     step_w2_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -82,7 +86,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    ws_produce<ZM != 0>(A, S, nitems, ns, full, empty, dful, desc, stage0);
     return;
   }
 
@@ -123,12 +127,16 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
 
   int s = 0;
   uint32_t par = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+  float2 zcarry[R];   // z-march: the right z face flux of the previous item, per row
+  ItemWalk<ZM != 0> wk;
+  for (wk.start(); wk.valid(nitems); wk.next(d.n[2])) {
     int sn = s + 1;
     uint32_t parn = par;
     if (sn == ns) { sn = 0; parn ^= 1u; }
     if (PF) {
-      if (it + gridDim.x < nitems) {
+      ItemWalk<ZM != 0> wn = wk;
+      wn.next(d.n[2]);
+      if (wn.valid(nitems)) {
         if (!ws_wait(&dful[sn], parn, A.status)) return;
         w2_load<R>(A, desc[sn], x0, y0, yrow, lane, nxt);
       }
@@ -202,13 +210,21 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
       for (int a = 2; a < 6; a++) {
         if (d.n[a] <= 1) continue;
         const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
-        const float2 Em2 = ld2(sN), Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
-        const float2 vr = cur.vr[a - 2][r], vl = cur.vl[a - 2][r];
+        const float2 Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
+        const float2 vr = cur.vr[a - 2][r];
         const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
-        const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
-        dEa -= (fra - fla) * kir[a - 2];
         const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
-        const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+        float fla, flb;
+        if (ZM && a == 2 && wk.z > 0) {   // left z face = the previous plane's right z face
+          fla = zcarry[r].x;
+          flb = zcarry[r].y;
+        } else {
+          const float2 Em2 = ld2(sN), vl = cur.vl[a - 2][r];
+          fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
+          flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+        }
+        if (ZM && a == 2) zcarry[r] = make_float2(fra, frb);
+        dEa -= (fra - fla) * kir[a - 2];
         dEb -= (frb - flb) * kir[a - 2];
       }
       const float mfa = e0.x * cur.lam[r].x, mfb = e0.y * cur.lam[r].y;

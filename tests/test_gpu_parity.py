@@ -73,7 +73,7 @@ SCHEDULES = [("tma", 8, 1024, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plan
              ("w2d", 4, 128, 0), ("w2d", 8, 256, 1), ("w3", 8, 256, 0), ("w3", 3, 512, 1),
              ("w3", 4, 128, 0), ("w4", 8, 512, 0), ("w4", 3, 256, 1), ("w4", 4, 128, 0), ("w5", 8, 512, 0),
              ("w5", 3, 256, 1), ("w5h", 4, 512, 0), ("w5h", 8, 256, 1), ("w6", 8, 256, 0), ("w6", 3, 512, 1),
-             ("cell", 8, 256, 0)]
+             ("w2z", 8, 512, 1), ("w2z", 3, 256, 0), ("cell", 8, 256, 0)]
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -220,7 +220,8 @@ def test_fp32_schedules_agree():
                                     ("w4", 4, 128, 1), ("w4", 4, 256, 0), ("w4", 8, 512, 1),
                                     ("w5", 4, 256, 1), ("w5", 8, 512, 0), ("w5h", 4, 128, 0),
                                     ("w5h", 4, 256, 1), ("w5h", 8, 512, 0), ("w6", 4, 256, 1),
-                                    ("w6", 8, 512, 0)],
+                                    ("w6", 8, 512, 0), ("w2z", 4, 256, 1), ("w2z", 8, 512, 0),
+                                    ("w2z", 4, 128, 0)],
                          ids=lambda t: "%s-b%d-t%d-s%d" % t)
 def test_fp32_persistent_matches_tma(n, tuning):
     """the persistent kernels (several items per CTA, short last band, up to
@@ -237,7 +238,7 @@ def test_fp32_persistent_matches_tma(n, tuning):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("variant", ["tma", "group", "plane", "pipe", "ws", "wsd", "w2", "w2d", "w3", "w4", "w5", "w5h", "w6", "cell"])
+@pytest.mark.parametrize("variant", ["tma", "group", "plane", "pipe", "ws", "wsd", "w2", "w2d", "w3", "w4", "w5", "w5h", "w6", "w2z", "cell"])
 def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
     after 200 steps of the all-axes shear case."""
