@@ -197,13 +197,16 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
         o1 += (long long)c[b] * d.ps[1][b];
       }
     }
+    // z-march past the column's first plane: the left z face flux is carried
+    // by the consumers, so the z-2 plane (lane 1) is not needed
+    const bool skip_zm2 = ZM && w.z > 0;
     const float* src = nullptr;
     if (lane < RT_NPLANE) {
       long long off = p0;
       bool go = true;
       if (lane > 0) {
         const int a = 2 + (lane - 1) / 4, i = (lane - 1) % 4;
-        go = d.n[a] > 1;
+        go = d.n[a] > 1 && !(lane == 1 && skip_zm2);
         if (go) off = nb_plane(d, c, a, i < 2 ? i - 2 : i - 1);
       }
       if (go) src = A.E + off;
@@ -225,7 +228,7 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
     __syncwarp();
     if (lane == 0) {
       mbar_arrive(&dful[s]);   // release: the descriptor (ordered by the __syncwarp) is visible to waiters
-      mbar_arrive_expect_tx(&full[s], nplanes * pbytes);
+      mbar_arrive_expect_tx(&full[s], (nplanes - (skip_zm2 && d.n[2] > 1 ? 1u : 0u)) * pbytes);
     }
     __syncwarp();
     if (src) {

@@ -31,8 +31,9 @@ struct W2Regs {
 };
 
 template <int R>
+// skip_vlz: the left z-face velocities are not needed (z-march, carried flux)
 __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& D, int x0, int y0,
-                                        const int yrow[R], int lane, W2Regs<R>& G) {
+                                        const int yrow[R], int lane, W2Regs<R>& G, bool skip_vlz = false) {
   const Dims& d = A.d;
   const int nx = d.n[0], ny = d.n[1];
   const long long p0 = D.p0;
@@ -46,7 +47,7 @@ __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& 
     for (int a = 2; a < 6; a++) {
       const bool act = d.n[a] > 1;
       G.vr[a - 2][r] = act ? ld2(A.vel[a] + o) : make_float2(0.f, 0.f);
-      G.vl[a - 2][r] = act ? ld2(D.vl[a - 2] + q) : make_float2(0.f, 0.f);
+      G.vl[a - 2][r] = (act && !(a == 2 && skip_vlz)) ? ld2(D.vl[a - 2] + q) : make_float2(0.f, 0.f);
     }
     G.lam[r] = ld2_stream(A.lam[0] + o);
     G.xl[r] = x0 == 0 ? D.b0x[yrow[r]] : (lane == 0 ? A.vel[0][o - 1] : 0.f);
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
       }
     } else {
       if (!ws_wait(&dful[s], par, A.status)) return;
-      w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur);
+      w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur, ZM && wk.z > 0);
     }
     const WsDesc& D = desc[s];
     const long long p0 = D.p0;
