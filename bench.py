@@ -392,8 +392,11 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["seconds"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "jet_large plain fp64 (bounded CPU sample)",
-                                             "sample_grid": "x".join(map(str, CPU_SAMPLE_N))},
+            "data": "synthetic", "config": {"workload": "jet_large 32^3x32^3 plain fp64, CFL 0.4",
+                                             "cells": 32 ** 6, "form": "fp64",
+                                             "sample_grid": "x".join(map(str, CPU_SAMPLE_N)),
+                                             "sample": "each step is a bounded sample: the same physics "
+                                                       "on the sample grid (the rate is per cell)"},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
