@@ -224,7 +224,7 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
     return out
 
 
-def bench_batched(steps, warmup, members=48, seed=2024, fixed=None):
+def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None):
     """48 independent fp32 instances (dims per axis from {8,16,24,32} spatial
     and {8,12,16,24} spectral, own N0, f, mean-flow amplitude, packet init)
     advanced by one persistent, graph-captured launch per step, with the
@@ -235,7 +235,8 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None):
     from raytracer_3d_gb300.autotune import tune_batch
     from raytracer_3d_gb300.batch import Batch
     rng = np.random.default_rng(seed)
-    exps = [configs.ensemble_member(rng, steps=500) for _ in range(members)]
+    kw = {"spatial": spatial} if spatial else {}
+    exps = [configs.ensemble_member(rng, steps=500, **kw) for _ in range(members)]
     t0 = time.perf_counter()
     models = []
     for e in exps:
@@ -324,7 +325,8 @@ def gpu_arm(args):
         return
     if args.only == "batch":   # profiling runs of the batched form only
         out = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,
-                            fixed=tuple(int(v) for v in args.batch_tuning.split(",")) if args.batch_tuning else None)
+                            fixed=tuple(int(v) for v in args.batch_tuning.split(",")) if args.batch_tuning else None,
+                            spatial=tuple(int(v) for v in args.batch_spatial.split(",")) if args.batch_spatial else None)
         if rank == 0:
             print(json.dumps({"profile_only": "fp32_batched", **out}), flush=True)
         return
@@ -424,6 +426,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--batch-members", type=int, default=48)
+    ap.add_argument("--batch-spatial", default=None, help="spatial extents of the members, e.g. 8,16 (profiling)")
     ap.add_argument("--batch-tuning", default=None,
                     help="band,threads,sweep,persistent[,slices] (skip the batch tuner)")
     ap.add_argument("--only", default="all", choices=("all", "batch", "serve"),

@@ -32,7 +32,12 @@ struct W6Desc {
   float zr[RT_W6_MAXG], zi[RT_W6_MAXG], zl[RT_W6_MAXG];  // z faces of every slice
 };
 __host__ __device__ constexpr size_t w6_desc_bytes() { return (sizeof(W6Desc) + 15) / 16 * 16; }
-__host__ __device__ constexpr size_t w6_head_bytes() { return 128 + RT_WS_MAXSTAGE * w6_desc_bytes(); }
+// the producer's shared-memory copy of the current member's arguments
+// (batched form: read once per member instead of from global memory per item)
+__host__ __device__ constexpr size_t w6_member_bytes() { return (sizeof(BatchMember<float>) + 15) / 16 * 16; }
+__host__ __device__ constexpr size_t w6_head_bytes() {
+  return 128 + RT_WS_MAXSTAGE * w6_desc_bytes() + w6_member_bytes();
+}
 
 // Stage layout, in floats, for G slices of an nx x ny plane (P = nx*ny):
 // the z window, then every k/l/m neighbour plane and every velocity / rate
@@ -423,15 +428,31 @@ __global__ void __launch_bounds__(NT + 32, 1)
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    int s = 0, j = 0;
+    int s = 0, j = 0, jcached = -1;
+    long long first_j = 0, first_next = mem ? first[1] : 0;
+    BatchMember<float>* mc =
+        reinterpret_cast<BatchMember<float>*>(smem_raw + 128 + RT_WS_MAXSTAGE * w6_desc_bytes());
     uint32_t rnd = 0;
     long long issued = 0;
     for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-      if (mem)
-        while (it >= first[j + 1]) j++;
-      const StepArgs<float>& Aj = mem ? mem[j].A : A;
-      const PlaneSched& Sj = mem ? mem[j].S : S;
-      const W6Prep P = w6_prepare(Aj, Sj, mem ? it - first[j] : it);
+      if (mem) {
+        while (it >= first_next) {
+          j++;
+          first_j = first_next;
+          first_next = first[j + 1];
+        }
+        if (j != jcached) {   // the 32 lanes copy the member's arguments into shared memory
+          const unsigned* src = reinterpret_cast<const unsigned*>(&mem[j]);
+          unsigned* dst = reinterpret_cast<unsigned*>(mc);
+          const int words = (int)(sizeof(BatchMember<float>) / sizeof(unsigned));
+          for (int k = threadIdx.x & 31; k < words; k += 32) dst[k] = src[k];
+          __syncwarp();
+          jcached = j;
+        }
+      }
+      const StepArgs<float>& Aj = mem ? mc->A : A;
+      const PlaneSched& Sj = mem ? mc->S : S;
+      const W6Prep P = w6_prepare(Aj, Sj, mem ? it - first_j : it);
       if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
       w6_commit(P, Sj.gz, j, stage0 + (size_t)s * stage_floats, &desc[s], &full[s], &dful[s]);
       issued++;
