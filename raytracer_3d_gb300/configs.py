@@ -4,9 +4,13 @@ and tested on.
 
 Each experiment is a plain description; `build_model` turns it into a
 `Model` by the reference's setup order (main.f90:36-47).  Inputs are seeded
-and synthetic.  Decisions where the workload text and the reference differ
-are listed in the design doc (open x/y boundaries instead of periodic, symmetric
-m grid, CFL-defined dt).
+and synthetic.  Where a workload description and the reference differ the
+reference wins: x and y boundaries are the reference's open outflow
+(integrate.f90:24-45; it has no periodic mode), spectral grids are centred
+on zero as calc_grid.f90:167-169 builds them (the z reflection reverses m,
+parallel_mpi.f90:839), and dt comes from a CFL number through the maximum
+cell rate (the reference sets dt by hand and only prints the CFL number,
+diagnose.f90:295-317).
 """
 from dataclasses import dataclass, field
 from typing import Callable, Optional, Tuple
