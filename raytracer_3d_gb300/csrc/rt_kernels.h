@@ -133,7 +133,8 @@ size_t w6_smem(int ns, long long stage_floats);
 int w6_blocks_per_sm(int threads, size_t smem);
 cudaError_t launch_batch_w6(const void* members, const long long* first, int nmem, int threads, int ns,
                             long long stage_floats, int grid, cudaStream_t st);
-// persistent binary32 kernels (rt_persist.cu); done = false when the tuning
+// persistent binary32 kernels (dispatch in rt_persist.cu; the families in
+// rt_persist.cu, rt_persist_w2.cu, rt_persist_ws.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);
 DiagSizes diag_sizes(const Dims& d);

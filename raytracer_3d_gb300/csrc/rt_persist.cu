@@ -1,187 +1,17 @@
 // rt_persist.cu -- launchers of the persistent binary32 step kernels:
-// the two-stage pipelined kernel (rt_step5.cuh, variant RT_VARIANT_PIPE) and
-// the warp-specialised multi-stage kernel (rt_step6.cuh, variants
-// RT_VARIANT_WS with register look-ahead and RT_VARIANT_WSD without) and
-// its 2-wide block form (rt_step7.cuh, RT_VARIANT_W2 / RT_VARIANT_W2D), and
-// the form with every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3),
-// the form with the producer folded into warp 0 (rt_step9.cuh,
-// RT_VARIANT_W4), and the row-chunk form with consumer groups (rt_step10.cuh,
-// RT_VARIANT_W5 with 256-thread groups, RT_VARIANT_W5H with 128), and the
-// small-plane form with z slices per item (rt_step11.cuh, RT_VARIANT_W6,
-// also for the ensemble class of small planes).
-// Kept in a translation unit of their own so the library builds in parallel.
-#include <algorithm>
-
-#include "rt_kernels.h"
-#include "rt_step11.cuh"
+// the dispatch over every persistent variant (launch_persist), the form with
+// every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3) single-field and
+// batched, and the small-plane form with z slices per item (rt_step11.cuh,
+// RT_VARIANT_W6, also the ensemble class of small planes).  The other
+// families are instantiated in rt_persist_w2.cu and rt_persist_ws.cu so the
+// library builds in parallel.
+#include "rt_persist.cuh"
 
 namespace rt {
 
 namespace {
 
-int most_cells(long long nxy, int nt) { return (int)((nxy + nt - 1) / nt); }
-
-template <class K>
-cudaError_t set_smem(K kernel, size_t bytes) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
-int sm_count() {
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  return nsm;
-}
-
-// one resident wave of persistent CTAs, at most one per item
-template <class K>
-cudaError_t persistent_grid(K kernel, int block, size_t smem, long long nitems, long long& grid) {
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  grid = std::min<long long>(nitems, (long long)per_sm * sm_count());
-  return cudaSuccess;
-}
-
-// ---- two-stage pipelined kernel ----
-template <int NT, int MAXC>
-cudaError_t launch_pipe_c(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const size_t sm = pipe_smem(A.d);
-  cudaError_t e = set_smem(step_pipe_kernel<NT, MAXC>, sm);
-  if (e != cudaSuccess) return e;
-  const long long nitems = dense_items(A.d);
-  long long grid = 0;
-  e = persistent_grid(step_pipe_kernel<NT, MAXC>, NT, sm, nitems, grid);
-  if (e != cudaSuccess) return e;
-  step_pipe_kernel<NT, MAXC><<<(unsigned)grid, NT, sm, st>>>(A, S, nitems);
-  return cudaGetLastError();
-}
-
-template <int NT>
-cudaError_t launch_pipe_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int mc = most_cells((long long)A.d.n[0] * A.d.n[1], NT);
-  if (mc <= 1) return launch_pipe_c<NT, 1>(A, S, st);
-  if (mc <= 2) return launch_pipe_c<NT, 2>(A, S, st);
-  return launch_pipe_c<NT, 4>(A, S, st);
-}
-
-bool pipe_ok(const Dims& d, int threads) {
-  return tma_ok<float>(d) && pipe_smem(d) <= 220 * 1024 &&
-         most_cells((long long)d.n[0] * d.n[1], threads) <= RT_TMA_MAXC && (long long)d.n[0] * d.n[1] <= 4096;
-}
-
-// ---- warp-specialised multi-stage kernel ----
-// rows per consumer thread: the thread columns are x = t % nx, so NT / nx
-// row chunks of R rows must cover ny
-int ws_rows(const Dims& d, int nt) {
-  const int nyc = nt / d.n[0];
-  if (nyc < 1) return 0;
-  const int R = (d.n[1] + nyc - 1) / nyc;
-  return R <= 1 ? 1 : (R <= 2 ? 2 : (R <= 4 ? 4 : 0));
-}
-int ws_max_smem() {
-  int dev = 0, v = 0;
-  cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
-  return v - 1024;
-}
-int ws_stages(const Dims& d) {
-  const long long room = (long long)ws_max_smem() - (long long)ws_head_bytes();
-  const long long per = (long long)ws_stage_bytes(d);
-  const long long ns = room > 0 ? room / per : 0;
-  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
-}
-bool ws_ok(const Dims& d, int threads) {
-  if (threads != 128 && threads != 256 && threads != 512) return false;
-  return d.n[0] >= 2 && d.n[1] >= 2 && tma_ok<float>(d) && d.n[0] <= threads && ws_rows(d, threads) > 0 &&
-         (long long)d.n[0] * d.n[1] <= 4096 && dense_items(d) < (1LL << 31) && ws_stages(d) >= 2;
-}
-
-template <int NT, int R, int PF>
-cudaError_t launch_ws_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int ns = ws_stages(A.d);
-  const size_t sm = ws_smem(A.d, ns);
-  cudaError_t e = set_smem(step_ws_kernel<NT, R, PF>, sm);
-  if (e != cudaSuccess) return e;
-  const long long nitems = dense_items(A.d);
-  long long grid = 0;
-  e = persistent_grid(step_ws_kernel<NT, R, PF>, NT + 32, sm, nitems, grid);
-  if (e != cudaSuccess) return e;
-  step_ws_kernel<NT, R, PF><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
-  return cudaGetLastError();
-}
-
-template <int NT, int PF>
-cudaError_t launch_ws_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int R = ws_rows(A.d, NT);
-  if (R == 1) return launch_ws_r<NT, 1, PF>(A, S, st);
-  if (R == 2) return launch_ws_r<NT, 2, PF>(A, S, st);
-  return launch_ws_r<NT, 4, PF>(A, S, st);
-}
-
-template <int PF>
-cudaError_t launch_ws_pf(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st) {
-  if (threads == 128) return launch_ws_nt<128, PF>(A, S, st);
-  if (threads == 256) return launch_ws_nt<256, PF>(A, S, st);
-  return launch_ws_nt<512, PF>(A, S, st);
-}
-
-// ---- 2-wide block kernel ----
-int w2_rows(const Dims& d, int nt) {
-  const int nyc = nt / (d.n[0] / 2);
-  if (nyc < 1) return 0;
-  const int R = (d.n[1] + nyc - 1) / nyc;
-  return R <= 1 ? 1 : (R <= 2 ? 2 : (R <= 4 ? 4 : 0));
-}
-bool w2_ok(const Dims& d, int threads) {
-  if (threads != 128 && threads != 256 && threads != 512) return false;
-  return d.n[0] >= 2 && d.n[0] % 2 == 0 && d.n[1] >= 2 && tma_ok<float>(d) && d.n[0] / 2 <= threads &&
-         w2_rows(d, threads) > 0 && (long long)d.n[0] * d.n[1] <= 4096 && dense_items(d) < (1LL << 31) &&
-         ws_stages(d) >= 2;
-}
-
-// ZM = 1: z-march, the count is the number of (k,l,m) columns
-template <int NT, int R, int PF, int ZM>
-cudaError_t launch_w2_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int ns = ws_stages(A.d);
-  const size_t sm = ws_smem(A.d, ns);
-  cudaError_t e = set_smem(step_w2_kernel<NT, R, PF, ZM>, sm);
-  if (e != cudaSuccess) return e;
-  const long long nitems = ZM ? (long long)A.d.n[3] * A.d.n[4] * A.d.n[5] : dense_items(A.d);
-  long long grid = 0;
-  e = persistent_grid(step_w2_kernel<NT, R, PF, ZM>, NT + 32, sm, nitems, grid);
-  if (e != cudaSuccess) return e;
-  step_w2_kernel<NT, R, PF, ZM><<<(unsigned)grid, NT + 32, sm, st>>>(A, S, nitems, ns);
-  return cudaGetLastError();
-}
-
-template <int NT, int PF, int ZM>
-cudaError_t launch_w2_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int R = w2_rows(A.d, NT);
-  if (R == 1) return launch_w2_r<NT, 1, PF, ZM>(A, S, st);
-  if (R == 2) return launch_w2_r<NT, 2, PF, ZM>(A, S, st);
-  return launch_w2_r<NT, 4, PF, ZM>(A, S, st);
-}
-
-template <int PF, int ZM = 0>
-cudaError_t launch_w2_pf(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st) {
-  if (threads == 128) return launch_w2_nt<128, PF, ZM>(A, S, st);
-  if (threads == 256) return launch_w2_nt<256, PF, ZM>(A, S, st);
-  return launch_w2_nt<512, PF, ZM>(A, S, st);
-}
-
 // ---- all operands staged ----
-int w3_stages(const Dims& d) {
-  const long long room = (long long)ws_max_smem() - (long long)ws_head_bytes();
-  const long long per = (long long)(w3_stage_floats(d) * sizeof(float));
-  const long long ns = room > 0 ? room / per : 0;
-  return (int)std::min<long long>(ns, RT_WS_MAXSTAGE);
-}
-bool w3_ok(const Dims& d, int threads) {
-  return w2_ok(d, threads) && d.n[0] % 4 == 0 && d.n[1] % 4 == 0 && w3_stages(d) >= 2;
-}
-
 template <int NT, int R>
 cudaError_t launch_w3_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
   const int ns = w3_stages(A.d);
@@ -202,84 +32,6 @@ cudaError_t launch_w3_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStre
   if (R == 1) return launch_w3_r<NT, 1>(A, S, st);
   if (R == 2) return launch_w3_r<NT, 2>(A, S, st);
   return launch_w3_r<NT, 4>(A, S, st);
-}
-
-// ---- producer in warp 0 ----
-template <int NT, int R>
-cudaError_t launch_w4_r(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int ns = ws_stages(A.d);
-  const size_t sm = ws_smem(A.d, ns);
-  cudaError_t e = set_smem(step_w4_kernel<NT, R>, sm);
-  if (e != cudaSuccess) return e;
-  const long long nitems = dense_items(A.d);
-  long long grid = 0;
-  e = persistent_grid(step_w4_kernel<NT, R>, NT, sm, nitems, grid);
-  if (e != cudaSuccess) return e;
-  step_w4_kernel<NT, R><<<(unsigned)grid, NT, sm, st>>>(A, S, nitems, ns);
-  return cudaGetLastError();
-}
-
-template <int NT>
-cudaError_t launch_w4_nt(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const int R = w2_rows(A.d, NT);
-  if (R == 1) return launch_w4_r<NT, 1>(A, S, st);
-  if (R == 2) return launch_w4_r<NT, 2>(A, S, st);
-  return launch_w4_r<NT, 4>(A, S, st);
-}
-
-// ---- row chunks, consumer groups ----
-// rows per thread R and rows per chunk hr for groups of gt threads: hr is a
-// multiple of 4 (16-byte rows of the face-0 copy), at least 4
-struct W5Shape {
-  int R = 0, hr = 0, nyc = 0, ns = 0;
-};
-W5Shape w5_shape(const Dims& d, int gt, int ng) {
-  W5Shape w;
-  const int nx = d.n[0], ny = d.n[1];
-  if (nx < 4 || nx % 4 || ny < 4 || ny % 4 || nx / 2 > gt) return w;
-  const int chunks = gt / (nx / 2);
-  for (int R = 1; R <= 2; R++) {
-    int hr = chunks * R / 4 * 4;
-    if (hr > ny) hr = ny;
-    if (hr >= 4) {
-      w.R = R;
-      w.hr = hr;
-      break;
-    }
-  }
-  if (!w.R) return w;
-  w.nyc = (ny + w.hr - 1) / w.hr;
-  W5Layout L{nx, w.hr};
-  const long long room = (long long)ws_max_smem() - (long long)w5_head_bytes();
-  const long long per = (long long)L.floats() * (long long)sizeof(float);
-  w.ns = (int)std::min<long long>(room > 0 ? room / per : 0, RT_WS_MAXSTAGE);
-  if (w.ns < ng + 1) w.R = 0;
-  return w;
-}
-bool w5_ok(const Dims& d, int gt, int threads) {
-  if (threads % gt || threads / gt < 1 || threads / gt > 4) return false;
-  const W5Shape w = w5_shape(d, gt, threads / gt);
-  return w.R > 0 && d.n[0] >= 4 && tma_ok<float>(d) && dense_items(d) * w.nyc < (1LL << 31);
-}
-
-template <int GT, int NG, int R>
-cudaError_t launch_w5_r(const StepArgs<float>& A, const PlaneSched& S, const W5Shape& w, cudaStream_t st) {
-  const size_t sm = w5_smem(A.d, w.hr, w.ns);
-  cudaError_t e = set_smem(step_w5_kernel<GT, NG, R>, sm);
-  if (e != cudaSuccess) return e;
-  const long long nitems = dense_items(A.d) * w.nyc;
-  long long grid = 0;
-  e = persistent_grid(step_w5_kernel<GT, NG, R>, GT * NG + 32, sm, nitems, grid);
-  if (e != cudaSuccess) return e;
-  step_w5_kernel<GT, NG, R><<<(unsigned)grid, GT * NG + 32, sm, st>>>(A, S, nitems, w.nyc, w.hr, w.ns);
-  return cudaGetLastError();
-}
-
-template <int GT, int NG>
-cudaError_t launch_w5_ng(const StepArgs<float>& A, const PlaneSched& S, cudaStream_t st) {
-  const W5Shape w = w5_shape(A.d, GT, NG);
-  if (w.R == 1) return launch_w5_r<GT, NG, 1>(A, S, w, st);
-  return launch_w5_r<GT, NG, 2>(A, S, w, st);
 }
 
 template <int NT, int R>
@@ -433,22 +185,17 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
   if (tn.variant == RT_VARIANT_W5 && w5_ok(A.d, 256, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.threads == 256) return launch_w5_ng<256, 1>(A, S, st);
-    return launch_w5_ng<256, 2>(A, S, st);
+    return launch_w5_family(A, S, 256, tn.threads, st);
   }
   if (tn.variant == RT_VARIANT_W5H && w5_ok(A.d, 128, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.threads == 128) return launch_w5_ng<128, 1>(A, S, st);
-    if (tn.threads == 256) return launch_w5_ng<128, 2>(A, S, st);
-    return launch_w5_ng<128, 4>(A, S, st);
+    return launch_w5_family(A, S, 128, tn.threads, st);
   }
   if (tn.variant == RT_VARIANT_W4 && w2_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.threads == 128) return launch_w4_nt<128>(A, S, st);
-    if (tn.threads == 256) return launch_w4_nt<256>(A, S, st);
-    return launch_w4_nt<512>(A, S, st);
+    return launch_w4_family(A, S, tn.threads, st);
   }
   if (tn.variant == RT_VARIANT_W3 && w3_ok(A.d, tn.threads)) {
     done = true;
@@ -461,27 +208,22 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
     done = true;
     // columns of z in band order over (k,l,m): units are k alone (gz = nz)
     const PlaneSched S = make_sched(A.d, tn, A.d.n[2]);
-    return launch_w2_pf<0, 1>(A, S, tn.threads, st);
+    return launch_w2_family(A, S, tn.threads, 0, 1, st);
   }
   if ((tn.variant == RT_VARIANT_W2 || tn.variant == RT_VARIANT_W2D) && w2_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.variant == RT_VARIANT_W2) return launch_w2_pf<1>(A, S, tn.threads, st);
-    return launch_w2_pf<0>(A, S, tn.threads, st);
+    return launch_w2_family(A, S, tn.threads, tn.variant == RT_VARIANT_W2 ? 1 : 0, 0, st);
   }
   if ((tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) && ws_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.variant == RT_VARIANT_WS) return launch_ws_pf<1>(A, S, tn.threads, st);
-    return launch_ws_pf<0>(A, S, tn.threads, st);
+    return launch_ws_family(A, S, tn.threads, tn.variant == RT_VARIANT_WS ? 1 : 0, st);
   }
   if (tn.variant == RT_VARIANT_PIPE && pipe_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
-    if (tn.threads == 128) return launch_pipe_nt<128>(A, S, st);
-    if (tn.threads == 512) return launch_pipe_nt<512>(A, S, st);
-    if (tn.threads == 1024) return launch_pipe_nt<1024>(A, S, st);
-    return launch_pipe_nt<256>(A, S, st);
+    return launch_pipe_family(A, S, tn.threads, st);
   }
   return cudaSuccess;
 }
