@@ -118,6 +118,23 @@ int rt_set_dt(rt_handle* h, double dt);
 int rt_set_state(rt_handle* h, const double* E);
 int rt_get_state(rt_handle* h, double* E);
 
+/* Bottom forcing of the forced configurations (the set_forcing hook,
+ * main.f90:69).  From the next rt_integrate on, every step first updates the
+ * bottom z plane (Fortran z index 1) of E in place, then integrates:
+ *   RT_FORCING_FLUX   E += dt*F/dzt(1)                  lee1.f90:193-212
+ *                     (F = flux_lee)
+ *   RT_FORCING_RELAX  E -= dt*max(0,zdot)*(E-F)/dzt(1)  critical_gm1.f90:119-139
+ *                     (F = E_gm; zdot from rt_calc_parameter)
+ * F is a padded 5D host array with axes x,y,k,l,m,
+ * (nx+4)(ny+4)(nk+4)(nl+4)(nm+4) doubles like the reference's allocatable;
+ * its interior is copied to the device.  RT_FORCING_NONE (F may be NULL)
+ * switches the forcing off.  rt_step_dry does not apply it; a batch applies
+ * each member's own forcing. */
+#define RT_FORCING_NONE 0
+#define RT_FORCING_FLUX 1
+#define RT_FORCING_RELAX 2
+int rt_set_forcing(rt_handle* h, int kind, const double* F);
+
 /* Replaces integrate (integrate.f90:4-271, called at main.f90:70):
  * nsteps forward-Euler steps on the device-resident state. */
 int rt_integrate(rt_handle* h, int nsteps);

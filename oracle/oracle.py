@@ -20,6 +20,7 @@ FIELDS6 = ("E", "dE", "xdot", "ydot", "zdot", "kdot", "ldot", "mdot", "omega_i",
 FIELDS3 = ("Nsqr", "U", "V", "E_int", "meanfl_int", "diss_ks", "diss_ke", "diss_ls",
            "diss_le", "diss_ms", "diss_me")
 AXES = ("x", "y", "z", "k", "l", "m")
+FORCING_NONE, FORCING_FLUX, FORCING_RELAX = 0, 1, 2   # ORC_FORCING_* of rt_oracle.h
 BUDGET = ("eint", "mflint", "mfl_max", "umax", "vmax", "wmax", "kmax", "lmax", "mmax",
           "bfl_xs", "bfl_xe", "bfl_ys", "bfl_ye", "bfl_zs", "bfl_ze",
           "bfl_ks", "bfl_ke", "bfl_ls", "bfl_le", "bfl_ms", "bfl_me",
@@ -62,6 +63,9 @@ def _load(threads):
     lib.orc_max_rate.restype = ctypes.c_double
     lib.orc_max_rate.argtypes = [P]
     lib.orc_threads.restype = ctypes.c_int
+    lib.orc_set_forcing.restype = ctypes.c_int
+    lib.orc_set_forcing.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.orc_apply_forcing.argtypes = [P]
     _libs[name] = lib
     return lib
 
@@ -118,6 +122,25 @@ class Oracle:
 
     def integrate(self, nsteps=1):
         self.lib.orc_integrate_n(self.s, int(nsteps))
+
+    def set_forcing(self, kind, F=None):
+        """set_forcing before every integrate: kind FORCING_NONE, FORCING_FLUX
+        (lee1.f90:193-212) or FORCING_RELAX (critical_gm1.f90:119-139); F is
+        the padded 5D field (x,y,k,l,m), Fortran order."""
+        ptr = None
+        if F is not None:
+            P5 = tuple(self.n[a] + 2 * ONX for a in (0, 1, 3, 4, 5))
+            F = np.asfortranarray(F, dtype=np.float64)
+            if F.shape != P5:
+                raise ValueError("forcing field must have the padded shape %s, got %s" % (P5, F.shape))
+            self._force = F
+            ptr = F.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        rc = self.lib.orc_set_forcing(self.s, int(kind), ptr)
+        if rc:
+            raise ValueError("orc_set_forcing failed (%d)" % rc)
+
+    def apply_forcing(self):
+        self.lib.orc_apply_forcing(self.s)
 
     def diagnose(self):
         b = _Budget()

@@ -32,6 +32,8 @@ struct orc_state {
   double* f6[ORC_N6D];
   double* f3[3 + 8];
   double* g1[24];
+  int forcing;       /* ORC_FORCING_* */
+  double* force;     /* padded 5D (x,y,k,l,m) forcing field */
 };
 
 /* Fortran index f (1-onx..n+onx) -> 0-based padded position */
@@ -90,6 +92,7 @@ void orc_destroy(orc_state* s) {
   for (int f = 0; f < ORC_N6D; f++) free(s->f6[f]);
   for (int f = 0; f < 11; f++) free(s->f3[f]);
   for (int f = 0; f < 24; f++) free(s->g1[f]);
+  free(s->force);
   free(s);
 }
 
@@ -495,8 +498,56 @@ void orc_integrate(orc_state* s) {
   }
 }
 
+/* ------------------------------------------------------------------------ */
+/* set_forcing of the forced configurations (called before integrate,         */
+/* main.f90:69-70); both act on the bottom z plane (Fortran k = 1) only        */
+/* ------------------------------------------------------------------------ */
+
+static long long len5(const orc_state* s) { return s->P[0] * s->P[1] * s->P[3] * s->P[4] * s->P[5]; }
+
+/* F(i,j,l,n,m) of a padded 5D array with axes x,y,k,l,m */
+static inline long long i5(const orc_state* s, int i, int j, int l, int n, int m) {
+  return PO(i) + s->P[0] * (PO(j) + s->P[1] * (PO(l) + s->P[3] * (PO(n) + s->P[4] * PO(m))));
+}
+
+int orc_set_forcing(orc_state* s, int kind, const double* F) {
+  if (kind != ORC_FORCING_NONE && kind != ORC_FORCING_FLUX && kind != ORC_FORCING_RELAX) return 1;
+  if (kind != ORC_FORCING_NONE && !F) return 1;
+  free(s->force);
+  s->force = NULL;
+  s->forcing = ORC_FORCING_NONE;
+  if (kind == ORC_FORCING_NONE) return 0;
+  s->force = (double*)malloc((size_t)len5(s) * sizeof(double));
+  if (!s->force) return 2;
+  memcpy(s->force, F, (size_t)len5(s) * sizeof(double));
+  s->forcing = kind;
+  return 0;
+}
+
+void orc_apply_forcing(orc_state* s) {
+  if (s->forcing == ORC_FORCING_NONE) return;
+  const int nx = s->n[0], ny = s->n[1], nk = s->n[3], nl = s->n[4], nm = s->n[5];
+  double* E = s->f6[ORC_E];
+  const double* zdot = s->f6[ORC_ZDOT];
+  const double dz = s->g1[4 * 2 + 2][PO(1)];   /* dzt(1) */
+  const double dt = s->dt;
+  const int k = 1;
+  for (int m = 1; m <= nm; m++) for (int n = 1; n <= nl; n++) for (int l = 1; l <= nk; l++)
+  for (int j = 1; j <= ny; j++) for (int i = 1; i <= nx; i++) {
+    const long long p = i6(s, i, j, k, l, n, m);
+    const double f = s->force[i5(s, i, j, l, n, m)];
+    if (s->forcing == ORC_FORCING_FLUX)
+      E[p] = E[p] + dt * f / dz;                                   /* lee1.f90:206 */
+    else
+      E[p] = E[p] - dt * fmax2(0., zdot[p]) * (E[p] - f) / dz;     /* critical_gm1.f90:132-133 */
+  }
+}
+
 void orc_integrate_n(orc_state* s, int nsteps) {
-  for (int t = 0; t < nsteps; t++) orc_integrate(s);
+  for (int t = 0; t < nsteps; t++) {
+    orc_apply_forcing(s);
+    orc_integrate(s);
+  }
 }
 
 /* ------------------------------------------------------------------------ */

@@ -69,7 +69,19 @@ void orc_calc_parameter(orc_state* s);
 /* integrate.f90:4-271 (+ reflection_condition, parallel_mpi.f90:798-876,
  * and superbee_fluxes.f90:4-174); one forward-Euler step */
 void orc_integrate(orc_state* s);
+/* nsteps of the main loop body (main.f90:69-70): set_forcing, then integrate */
 void orc_integrate_n(orc_state* s, int nsteps);
+
+/* set_forcing of the forced configurations, on the bottom z plane k = 1:
+ * FLUX  E += dt*F/dzt(1)                    (lee1.f90:193-212, F = flux_lee)
+ * RELAX E -= dt*max(0,zdot)*(E-F)/dzt(1)    (critical_gm1.f90:119-139, F = E_gm)
+ * F is a padded 5D array with axes x,y,k,l,m (the reference's allocatable
+ * flux_lee / E_gm, onx ghosts on every axis); it is copied.  NONE switches
+ * the forcing off.  Returns 0, 1 for a bad argument, 2 when out of memory. */
+enum { ORC_FORCING_NONE = 0, ORC_FORCING_FLUX = 1, ORC_FORCING_RELAX = 2 };
+int orc_set_forcing(orc_state* s, int kind, const double* F);
+/* one application of the forcing (no-op when NONE) */
+void orc_apply_forcing(orc_state* s);
 /* budget part of diagnose.f90:20-329; fills orc_budget and the 3D fields */
 void orc_diagnose(orc_state* s, orc_budget* out);
 /* dt helper for the CFL-defined configs: max over interior cells of

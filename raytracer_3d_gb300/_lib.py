@@ -16,6 +16,7 @@ RT_FP32 = 1
 
 RT_F_XDOT, RT_F_YDOT, RT_F_ZDOT, RT_F_KDOT, RT_F_LDOT, RT_F_MDOT = range(6)
 RT_F_LAMBDA_X, RT_F_LAMBDA_Y, RT_F_LAMBDA_Z, RT_F_LAMBDA = 6, 7, 8, 9
+RT_FORCING_NONE, RT_FORCING_FLUX, RT_FORCING_RELAX = 0, 1, 2
 
 
 class RtDims(ctypes.Structure):
@@ -56,6 +57,7 @@ SIGNATURES = {
     "rt_set_state": (ctypes.c_int, [_P, _D]),
     "rt_get_state": (ctypes.c_int, [_P, _D]),
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_set_forcing": (ctypes.c_int, [_P, ctypes.c_int, _D]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_state_interior": (ctypes.c_int, [_P, _P]),
     "rt_get_state_interior": (ctypes.c_int, [_P, _P]),

@@ -12,6 +12,7 @@ parallel_mpi.f90:839), and dt comes from a CFL number through the maximum
 cell rate (the reference sets dt by hand and only prints the CFL number,
 diagnose.f90:295-317).
 """
+import math
 from dataclasses import dataclass, field
 from typing import Callable, Optional, Tuple
 
@@ -46,6 +47,9 @@ class Experiment:
     fixed: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     seed: int = 1234
     meta: dict = field(default_factory=dict)
+    # set_forcing of the forced configurations: (model) -> (kind, F) with
+    # kind "flux" or "relax" and F the padded 5D field (x,y,k,l,m)
+    forcing: Optional[Callable] = None
 
     @property
     def cells(self):
@@ -68,6 +72,9 @@ def build_model(exp, precision="fp64", padded=True):
     m.calc_parameter()
     if exp.cfl is not None:
         m.set_dt(exp.cfl / m.max_rate())
+    if exp.forcing is not None:
+        kind, F = exp.forcing(m)
+        m.set_forcing(kind, F)
     m.set_state()
     return m
 
@@ -233,6 +240,138 @@ def section_2d(fac=1, steps=3):
 
     return Experiment("section_2d", n, d, f0, background, initial, steps, dt=40.0 / fac,
                       fixed=(f32(1e-3), 0.0, 0.0))
+
+
+# ---------------------------------------------------------------------------
+# the reference's forced configurations (for_config/lee1.f90,
+# critical_gm1.f90): a bottom forcing applied before every step
+# ---------------------------------------------------------------------------
+def _bottom_fill(m, f):
+    """U / V ghost planes below z = 1 and above z = nz copy the edge planes
+    (lee1.f90:74-85, critical_gm1.f90:70-79)."""
+    nz = m.n[2]
+    for arr in f:
+        for k in range(ONX):
+            arr[:, :, k] = arr[:, :, ONX]
+            arr[:, :, ONX + nz + k] = arr[:, :, ONX + nz - 1]
+
+
+def _forcing_mesh(m):
+    """kt(l), lt(n), mt(m), dmt(m) on the padded 5D (x,y,k,l,m) shape."""
+    P = [m.n[a] + 2 * ONX for a in range(6)]
+    kt = m.grid["k"]["t"].reshape(1, 1, P[3], 1, 1)
+    lt = m.grid["l"]["t"].reshape(1, 1, 1, P[4], 1)
+    mt = m.grid["m"]["t"].reshape(1, 1, 1, 1, P[5])
+    dmt = m.grid["m"]["dt"].reshape(1, 1, 1, 1, P[5])
+    return P, kt, lt, mt, dmt
+
+
+def lee_wave_flux(fac=2, steps=3, nz=20):
+    """lee1: nz=20, nk=24*fac, nm=26*fac, nx=ny=nl=1; mean flow and N of the
+    lee-wave setup and the bottom lee-wave energy flux flux_lee added to the
+    z = 1 plane every step (lee1.f90:14-229).  Default-real literals are
+    evaluated as the reference does (binary32 where the whole expression is
+    default real)."""
+    nk, nm = int(24 * fac), int(26 * fac)
+    f0 = f32(1e-4)
+    Lz, Ly, Lx = f32(2000.0), 240e3, 240e3
+    n = (1, 1, nz, nk, 1, nm)
+    # lee1.f90:46-51: dkt = 0.004/nk*2 etc. are default-real expressions
+    dk = float(np.float32(0.004) / np.float32(nk) * np.float32(2))
+    dl = float(np.float32(0.02) / np.float32(nk) * np.float32(2))
+    dm = float(np.float32(0.07) / np.float32(nm) * np.float32(2))
+    d = [np.full(1, Lx / 1), np.full(1, Ly / 1), np.full(nz, Lz / nz),
+         np.full(nk, dk), np.full(1, dl), np.full(nm, dm)]
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.U[:] = f32(0.1) + f32(0.10) * (1 + np.tanh((Z + 750) / 150)) / 2.0
+        m.Nsqr[:] = np.square(f32(2e-4) + f32(30e-4) * np.exp(Z / 800.0))
+        m.V[:] = 0.0
+        _bottom_fill(m, (m.U, m.V))
+
+    def initial(m, rng):
+        m.E[:] = 0.0
+
+    def forcing(m):
+        # lee1.f90:102-132 on the bottom plane k = 1, m from 0 (ms-onx+1)
+        P, kt, lt, mt, dmt = _forcing_mesh(m)
+        h_rms, nu, k_s = 10.0, f32(0.8), float(np.float32(1) / np.float32(10e3))
+        U1 = m.U[:, :, ONX].reshape(P[0], P[1], 1, 1, 1)
+        V1 = m.V[:, :, ONX].reshape(P[0], P[1], 1, 1, 1)
+        N1 = m.Nsqr[:, :, ONX].reshape(P[0], P[1], 1, 1, 1)
+        kh = np.sqrt(kt * kt + lt * lt)
+        om = -(kt * U1 + lt * V1)
+        om2 = om * om
+        ok = (om2 > f0 * f0) & (om2 < N1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            m_lee = -kh * np.sqrt(N1 - om2) / np.sqrt(om2 - f0 * f0)
+            F_top = h_rms * h_rms * nu / (PI_F * (k_s * k_s)) / np.power(1.0 + (kh / k_s) * (kh / k_s), nu + 1.0)
+            freq_fac = 4 * (PI_F * PI_F) * np.sqrt(N1 - om2) * np.sqrt(om2 - f0 * f0) * np.abs(om) / kh
+            dd = mt - m_lee
+            tw = 2 * dmt
+            flux = freq_fac * F_top * np.exp(-(dd * dd) / (tw * tw)) / (2 * dmt * np.sqrt(PI_F))
+        ok = ok & np.ones(P[:2] + P[3:], dtype=bool)
+        ok[:, :, :, :, 0] = False        # the m loop starts at ms-onx+1
+        F = np.zeros(P[:2] + P[3:], order="F")
+        F[ok] = np.broadcast_to(flux, F.shape)[ok]
+        return "flux", F
+
+    return Experiment("lee_wave_flux", n, d, f0, background, initial, steps, dt=300.0 / fac,
+                      fixed=(0.0, 0.0, 0.0), forcing=forcing)
+
+
+def critical_gm_relax(fac=1.0, steps=3):
+    """critical_gm1: nz=160*fac, nm=300*fac, the other axes 1, k_fixed=25.5e-3,
+    open z boundaries; the bottom plane relaxes towards a Garrett-Munk
+    spectrum E_gm where the z velocity points upward (critical_gm1.f90:11-141)."""
+    nz, nm = int(160 * fac), int(300 * fac)
+    f0 = f32(1e-4)
+    Lz, Ly, Lx = f32(2000.0), 100e3, 100e3
+    n = (1, 1, nz, 1, 1, nm)
+    d = [np.full(1, Lx / 1), np.full(1, Ly / 1), np.full(nz, Lz / nz),
+         np.full(1, f32(0.5e-3)), np.full(1, f32(0.5e-3)), np.full(nm, 2 * PI_F / Lz / 2.0)]
+    # (30e-4)**2 is a default-real expression (critical_gm1.f90:64)
+    N2 = float(np.float32(30e-4) * np.float32(30e-4))
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.Nsqr[:] = N2
+        m.U[:] = f32(0.2) * np.exp(-((Z + 1000) * (Z + 1000)) / 200 ** 2)
+        m.V[:] = 0.0
+        _bottom_fill(m, (m.U,))
+
+    def initial(m, rng):
+        m.E[:] = 0.0
+
+    def forcing(m):
+        # critical_gm1.f90:85-113 on the bottom plane k = 1
+        P, kt, lt, mt, dmt = _forcing_mesh(m)
+        g = np.float32(math.gamma(0.5))
+        na = float(np.float32(2) * np.float32(1.0) / g / g)   # default-real expression
+        nb = 2.0 / PI_F
+        E0, jstar = 3e-3, 10
+        c1 = 0.0
+        dz = m.grid["z"]["dt"]
+        for k in range(ONX, ONX + nz):
+            c1 = c1 + np.sqrt(m.Nsqr[ONX, ONX, k]) * dz[k] / PI_F
+        cstar = c1 / jstar
+        N1 = m.Nsqr[:, :, ONX].reshape(P[0], P[1], 1, 1, 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            kh = np.sqrt(kt * kt + lt * lt)
+            om = np.sqrt((N1 * (kh * kh) + (f0 * f0) * (mt * mt)) / (kh * kh + mt * mt))
+            t = N1 - om * om
+            Jac = t * t / ((mt * mt) * om * (N1 - f0 * f0))
+            mstar = np.sqrt(N1 - om * om) / cstar
+            r = mt / mstar
+            funcA = na / (1.0 + r * r)
+            funcB = nb * abs(f0) / (om * np.sqrt(om * om - f0 * f0))
+            Egm = E0 * funcA / mstar * funcB * Jac
+        F = np.asfortranarray(np.broadcast_to(Egm, P[:2] + P[3:]))
+        return "relax", F
+
+    return Experiment("critical_gm_relax", n, d, f0, background, initial, steps, dt=30.0,
+                      upper=False, lower=False, fixed=(f32(25.5e-3), 0.0, 0.0), forcing=forcing)
 
 
 # ---------------------------------------------------------------------------

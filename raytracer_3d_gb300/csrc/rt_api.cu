@@ -46,6 +46,10 @@ struct rt_handle {
   double* ucl[6]{};             // and of the face-0 planes
   void* E[2]{};
   int cur = 0;
+  int forcing = RT_FORCING_NONE;  // set_forcing before every step (rt_set_forcing)
+  double* force = nullptr;      // its interior 5D field (x,y,k,l,m)
+  long long force_gen = 0;      // changes with every rt_set_forcing
+  double dzt1 = 0.0;            // dzt(1), the bottom cell's spacing
   double* scratch = nullptr;    // reductions
   long long scratch_len = 0;
   double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
@@ -202,6 +206,16 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   return A;
 }
 
+// set_forcing on the state about to be stepped (main.f90:69)
+static cudaError_t apply_forcing(rt_handle* h, int buf, cudaStream_t st) {
+  const double dzt1 = h->dzt1;
+  if (h->p.precision == RT_FP64)
+    return launch_forcing<double>((double*)h->E[buf], h->force, (const double*)h->vel[2], h->d, h->p.dt, dzt1,
+                                  h->forcing, st);
+  return launch_forcing<float>((float*)h->E[buf], h->force, (const float*)h->vel[2], h->d, h->p.dt, dzt1,
+                               h->forcing, st);
+}
+
 // binary64 form: refresh the cached uCFL fields (after the coefficients or dt change)
 static int refresh_ucfl(rt_handle* h) {
   if (h->p.precision != RT_FP64 || !h->have_coeff) return RT_OK;
@@ -243,6 +257,8 @@ static int check_status(rt_handle* h) {
 struct rt_batch {
   std::vector<rt_handle*> mem;
   std::vector<int> cur0;        // members' ping-pong index when the arrays were built
+  std::vector<int> forced;      // members with a forcing, when the arrays were built
+  std::vector<long long> fgen;  // and every member's forcing generation then
   int fp64 = 0;
   int parity = 0;               // steps taken since the arrays were built, mod 2
   cudaStream_t st = nullptr;
@@ -304,13 +320,20 @@ static void batch_free_graphs(rt_batch* b) {
 
 // kernel launches per batch step
 static int batch_kernels(const rt_batch* b) {
-  return (b->np > 0 ? 1 : 0) + (b->ns6 > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0);
+  return (int)b->forced.size() + (b->np > 0 ? 1 : 0) + (b->ns6 > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0);
 }
 
-// one step of every member, starting from the arrays of parity `par`
+// one step of every member, starting from the arrays of parity `par`;
+// force = false leaves out the members' forcing (dry steps)
 template <class T>
-static cudaError_t batch_launch(rt_batch* b, int par) {
+static cudaError_t batch_launch(rt_batch* b, int par, bool force = true) {
   cudaError_t e = cudaSuccess;
+  // each member's set_forcing first (main.f90:69), on the state of this parity
+  if (force)
+    for (int j : b->forced) {
+      e = apply_forcing(b->mem[j], b->cur0[j] ^ par, b->st);
+      if (e != cudaSuccess) return e;
+    }
   if (b->np)
     e = launch_batch_w3(b->d_pmem[par], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage, b->pgrid, b->st);
   if (e == cudaSuccess && b->ns6)
@@ -506,6 +529,12 @@ static int batch_build(rt_batch* b) {
     b->grid = (int)std::min<long long>(items, (long long)per_sm * nsm);
   }
   b->parity = 0;
+  b->forced.clear();
+  b->fgen.assign(b->mem.size(), 0);
+  for (size_t j = 0; j < b->mem.size(); j++) {
+    if (b->mem[j]->forcing != RT_FORCING_NONE) b->forced.push_back((int)j);
+    b->fgen[j] = b->mem[j]->force_gen;
+  }
   // capture graph_steps launches starting at each parity
   batch_free_graphs(b);
   for (int start = 0; start < 2; start++) {
@@ -528,8 +557,10 @@ static int batch_build(rt_batch* b) {
 template <class T>
 static int batch_run(rt_batch* b, int nsteps) {
   const int n = (int)b->mem.size();
-  for (int j = 0; j < n; j++)  // a member stepped on its own since the build
-    if (b->mem[j]->cur != (b->cur0[j] ^ b->parity)) b->dirty = true;
+  for (int j = 0; j < n; j++)  // a member stepped on its own, or its forcing changed, since the build
+    if (b->mem[j]->cur != (b->cur0[j] ^ b->parity) || b->fgen.size() != (size_t)n ||
+        b->mem[j]->force_gen != b->fgen[j])
+      b->dirty = true;
   // the batch stream runs after everything queued on the members' streams
   for (int j = 0; j < n; j++) {
     BCUDA_TRY(b, cudaEventRecord(b->mem[j]->ev, b->mem[j]->st));
@@ -683,9 +714,10 @@ int rt_batch_dry(rt_batch* b, int nsteps) {
     if (rc) return rc;
   }
   for (int t = 0; t < nsteps; t++) {
-    cudaError_t e = b->fp64 ? batch_launch<double>(b, b->parity) : batch_launch<float>(b, b->parity);
+    cudaError_t e =
+        b->fp64 ? batch_launch<double>(b, b->parity, false) : batch_launch<float>(b, b->parity, false);
     if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
-    b->launches += batch_kernels(b);
+    b->launches += batch_kernels(b) - (long long)b->forced.size();
   }
   BCUDA_TRY(b, cudaEventRecord(b->ev, b->st));
   for (int j = 0; j < n; j++) {
@@ -821,6 +853,7 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->vol3);
   cudaFree(h->result);
   cudaFree(h->status);
+  cudaFree(h->force);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->ev) cudaEventDestroy(h->ev);
   if (h->st) cudaStreamDestroy(h->st);
@@ -843,6 +876,7 @@ int rt_set_grid(rt_handle* h, const double* dxt, const double* dyt, const double
           return fail(h, RT_ERR_GRID, "rt_set_grid: spacing %d at padded index %lld is not > 0", k, i);
     CUDA_TRY(h, cudaMemcpy(h->grid + h->goff[k], src[k], n * sizeof(double), cudaMemcpyHostToDevice));
   }
+  h->dzt1 = dzt[pidx(1)];
   int rc = upload_tab32(h);
   if (rc) return rc;
   h->have_grid = true;
@@ -1102,6 +1136,40 @@ int rt_host_direct(rt_handle* h) {
   return use_host_direct(h) ? 1 : 0;
 }
 
+int rt_set_forcing(rt_handle* h, int kind, const double* F) {
+  if (!h) return RT_ERR_ARG;
+  if (kind != RT_FORCING_NONE && kind != RT_FORCING_FLUX && kind != RT_FORCING_RELAX)
+    return fail(h, RT_ERR_ARG, "rt_set_forcing: unknown kind %d", kind);
+  if (kind != RT_FORCING_NONE && !F) return fail(h, RT_ERR_ARG, "rt_set_forcing: NULL forcing field");
+  const Dims& d = h->d;
+  const long long nplane = (long long)d.n[0] * d.n[1] * d.nspec;
+  // the work on the stream may still read the old field
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  h->force_gen += 1;
+  h->forcing = RT_FORCING_NONE;
+  if (kind == RT_FORCING_NONE) return RT_OK;
+  if (!h->force) {
+    int rc = dev_alloc(h, (void**)&h->force, (size_t)nplane * sizeof(double));
+    if (rc) return rc;
+  }
+  // interior of the padded 5D field (x,y,k,l,m), x fastest
+  const long long P0 = padded_len(d, 0), P1 = padded_len(d, 1), P3 = padded_len(d, 3), P4 = padded_len(d, 4);
+  std::vector<double> f((size_t)nplane);
+  long long q = 0;
+  for (int m = 0; m < d.n[5]; m++)
+    for (int n = 0; n < d.n[4]; n++)
+      for (int l = 0; l < d.n[3]; l++)
+        for (int j = 0; j < d.n[1]; j++) {
+          const double* row =
+              F + RT_ONX + P0 * ((j + RT_ONX) + P1 * ((l + RT_ONX) + P3 * ((n + RT_ONX) + P4 * (long long)(m + RT_ONX))));
+          std::memcpy(&f[(size_t)q], row, (size_t)d.n[0] * sizeof(double));
+          q += d.n[0];
+        }
+  CUDA_TRY(h, cudaMemcpy(h->force, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice));
+  h->forcing = kind;
+  return RT_OK;
+}
+
 int rt_integrate(rt_handle* h, int nsteps) {
   if (!h) return RT_ERR_ARG;
   if (nsteps < 0) return fail(h, RT_ERR_ARG, "rt_integrate: nsteps < 0");
@@ -1109,6 +1177,11 @@ int rt_integrate(rt_handle* h, int nsteps) {
   if (!h->have_state) return fail(h, RT_ERR_STATE, "rt_integrate: rt_set_state first");
   for (int t = 0; t < nsteps; t++) {
     cudaError_t e;
+    if (h->forcing != RT_FORCING_NONE) {
+      e = apply_forcing(h, h->cur, h->st);
+      h->launches += 1;
+      if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "forcing launch: %s", cudaGetErrorString(e));
+    }
     if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->tune, h->st);
     else e = launch_step<float>(make_step_args<float>(h, h->cur), h->tune, h->st);
     h->launches += 1;

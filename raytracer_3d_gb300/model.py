@@ -161,6 +161,28 @@ class Model:
         self._check(self._lib.rt_get_state(self._h, _lib.dptr(self.E)), "rt_get_state")
         return self.E
 
+    # ---- bottom forcing (set_forcing, main.f90:69) ------------------------------
+    FORCING = {"none": _lib.RT_FORCING_NONE, "flux": _lib.RT_FORCING_FLUX, "relax": _lib.RT_FORCING_RELAX}
+
+    def forcing_shape(self):
+        """Padded shape of a forcing field: axes x,y,k,l,m."""
+        return tuple(self.n[a] + 2 * ONX for a in (0, 1, 3, 4, 5))
+
+    def set_forcing(self, kind, F=None):
+        """Apply a bottom forcing before every following step: kind "flux"
+        (E += dt*F/dzt(1), lee1.f90:193-212), "relax" (E -= dt*max(0,zdot)*
+        (E-F)/dzt(1), critical_gm1.f90:119-139) or "none".  F is the padded
+        5D field with axes x,y,k,l,m (forcing_shape()), Fortran order."""
+        code = self.FORCING[kind] if isinstance(kind, str) else int(kind)
+        ptr = None
+        if code != _lib.RT_FORCING_NONE:
+            F = np.asfortranarray(F, dtype=np.float64)
+            if F.shape != self.forcing_shape():
+                raise ValueError("forcing field must have the padded shape %s, got %s"
+                                 % (self.forcing_shape(), F.shape))
+            ptr = _lib.dptr(F)
+        self._check(self._lib.rt_set_forcing(self._h, code, ptr), "rt_set_forcing")
+
     # ---- time stepping (main.f90:64-79) ----------------------------------------
     def integrate(self, nsteps=1):
         """integrate (integrate.f90:4-271), nsteps times, state on the GPU."""

@@ -9,9 +9,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-from oracle.oracle import Oracle  # noqa: E402
+from oracle.oracle import FORCING_FLUX, FORCING_RELAX, Oracle  # noqa: E402
 from raytracer_3d_gb300 import configs  # noqa: E402
 from raytracer_3d_gb300.grid import ONX  # noqa: E402
+
+
+FORCING_CODES = {"flux": FORCING_FLUX, "relax": FORCING_RELAX}
 
 
 def build_oracle(exp, threads=False):
@@ -31,6 +34,9 @@ def build_oracle(exp, threads=False):
         o.dt = dt
     else:
         o.dt = exp.dt
+    if exp.forcing is not None:
+        kind, F = exp.forcing(o)
+        o.set_forcing(FORCING_CODES[kind], F)
     return o
 
 
