@@ -18,6 +18,7 @@ from typing import Callable, Optional, Tuple
 
 import numpy as np
 
+from . import grid
 from .grid import ONX
 from .model import Model, zeros_padded
 
@@ -372,6 +373,75 @@ def critical_gm_relax(fac=1.0, steps=3):
 
     return Experiment("critical_gm_relax", n, d, f0, background, initial, steps, dt=30.0,
                       upper=False, lower=False, fixed=(f32(25.5e-3), 0.0, 0.0), forcing=forcing)
+
+
+# ---------------------------------------------------------------------------
+# stretched grids (for_config/gm1.f90, brava.f90): non-uniform spacings
+# ---------------------------------------------------------------------------
+def gm_column(fac=1, steps=3):
+    """gm1: nz=60*fac, nm=80*fac, the other axes 1, k_fixed=50e-3; the m
+    spacing is refined towards m=0 and mirrored (gm1.f90:33-49); the initial
+    state is a Garrett-Munk spectrum (gm1.f90:52-114)."""
+    nz, nm = int(60 * fac), int(80 * fac)
+    f0 = f32(1e-4)
+    Lz, Ly, Lx = f32(2000.0), 240e3, 240e3
+    n = (1, 1, nz, 1, 1, nm)
+    dm = grid.symmetric_stretched(nm, -1.0, lo=1e-6, hi=1e-1)
+    d = [np.full(1, Lx / 1), np.full(1, Ly / 1), np.full(nz, Lz / nz),
+         np.full(1, PI_F / Lx), np.full(1, PI_F / Ly), dm]
+    N = 30 * f0                      # N_func, gm1.f90:59
+
+    def background(m):
+        X, Y, Z = _mesh3(m)
+        m.U[:] = f32(0.10) * (1 + np.tanh((Z + 750) / 150)) / 2.0
+        m.Nsqr[:] = N * N
+        m.V[:] = 0.0
+        _bottom_fill(m, (m.U,))
+
+    def initial(m, rng):
+        # gm1.f90:87-114, evaluated on the interior
+        sl = _interior(m)
+        g = np.float32(math.gamma(0.5))
+        na = float(np.float32(2) * np.float32(1.0) / g / g)   # default-real expression
+        nb, E0, jstar = 2.0 / PI_F, 3e-3, 15.0
+        dz = m.grid["z"]["dt"]
+        c1 = 0.0
+        for k in range(ONX, ONX + nz):
+            c1 = c1 + N * dz[k] / PI_F
+        cstar = c1 / jstar
+        kt = m.grid["k"]["t"][ONX]
+        lt = m.grid["l"]["t"][ONX]
+        mt = m.grid["m"]["t"][ONX:ONX + nm]
+        kh2 = kt * kt + lt * lt
+        om = np.sqrt((N * N * kh2 + (f0 * f0) * (mt * mt)) / (kh2 + mt * mt))
+        t = N * N - om * om
+        Jac = t * t / ((mt * mt) * om * (N * N - f0 * f0))
+        mstar = np.sqrt(N * N - om * om) / cstar
+        r = mt / mstar
+        funcA = na / (1.0 + r * r)
+        funcB = nb * abs(f0) / (om * np.sqrt(om * om - f0 * f0))
+        spec = E0 * funcA / mstar * funcB * Jac * N / N / (4 * PI_F)
+        m.E[sl] = np.broadcast_to(spec.reshape(1, 1, 1, 1, 1, nm), n)
+
+    return Experiment("gm_column", n, d, f0, background, initial, steps, dt=20.0 / fac,
+                      fixed=(f32(50e-3), 0.0, 0.0))
+
+
+def stretched_mini(n=(8, 6, 8, 6, 6, 8), steps=3, seed=11, upper=True, lower=True, cfl=0.4):
+    """The all-axes shear case on non-uniform grids: x spacing growing
+    geometrically, y spacing jittered, z refined upward (brava.f90 zgrid),
+    k, l, m refined towards zero and mirrored (gm1.f90 / brava.f90 mgrid,
+    lgrid)."""
+    nx, ny, nz, nk, nl, nm = n
+    Lx, Ly, Lz = 30e3, 25e3, 3000.0
+    gx = 1.15 ** np.arange(nx)
+    jit = 1.0 + 0.3 * np.sin(1.7 * np.arange(ny) + 0.4)
+    d = [Lx * gx / gx.sum(), Ly * jit / jit.sum(), grid.bottom_refined(nz, Lz),
+         grid.symmetric_stretched(nk, -2e-3), grid.symmetric_stretched(nl, -2e-3),
+         grid.symmetric_stretched(nm, -5e-2)]
+    base = shear_mini(n=n, steps=steps, seed=seed, upper=upper, lower=lower, cfl=cfl)
+    return Experiment("stretched_mini", tuple(n), d, base.f0, base.background, base.initial, steps, cfl=cfl,
+                      seed=seed, upper=upper, lower=lower)
 
 
 # ---------------------------------------------------------------------------

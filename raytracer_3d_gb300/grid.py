@@ -34,6 +34,102 @@ def u_centered_grid(dyt):
     return dyu, yt, yu
 
 
+# ---------------------------------------------------------------------------
+# stretched grids of the reference's configurations (for_config/gm1.f90:33-49,
+# brava.f90:32-58): the spacing falls as 1 - 0.8*x**1.5 along a half axis and
+# its scale d0 is the root of a closure condition, found by bisection.  The
+# reference evaluates these in default real, so they are computed in binary32
+# here too and widened to binary64 at the end.
+# ---------------------------------------------------------------------------
+F32 = np.float32
+
+
+def bisect(f, lo, hi, tol, max_halvings=40):
+    """Root of the increasing-or-decreasing function f on [lo, hi] by the
+    bisection method in binary32 arithmetic.  The bracket is halved until
+    its nominal width (halved exactly each time, so that it keeps shrinking
+    below the binary32 spacing of the root) is below tol; returns the
+    bracket end at which f <= 0.  Raises GridError when [lo, hi] does not
+    bracket a sign change or when max_halvings are not enough."""
+    lo, hi = F32(lo), F32(hi)
+    flo, fhi = f(lo), f(hi)
+    if not (flo < 0) ^ (fhi < 0):
+        raise GridError("bisection: the interval [%g, %g] does not bracket a root" % (lo, hi))
+    below, above = (lo, hi) if flo < 0 else (hi, lo)     # f(below) < 0 <= f(above)
+    width = F32(above - below)
+    for _ in range(max_halvings):
+        width = F32(width * F32(0.5))
+        mid = F32(below + width)
+        fm = f(mid)
+        if fm <= 0:
+            below = mid
+        if abs(width) < tol or fm == 0:
+            return below
+    raise GridError("bisection: no convergence after %d halvings" % max_halvings)
+
+
+def stretched_half(d0, start, count):
+    """Positions p(0..count) and spacings d(1..count) (index 0 unused) of
+    the stretched half axis: p(0) = start, d(i) = d0*(1 - x(i)**1.5*0.8)
+    with x(i) = (i-1)/(count-1), p(i) = p(i-1) + d(i), in binary32
+    (gm1.f90 mgrid/lgrid, brava.f90 zgrid)."""
+    if count < 2:
+        raise GridError("a stretched half axis needs at least 2 cells")
+    p = np.zeros(count + 1, dtype=F32)
+    d = np.zeros(count + 1, dtype=F32)
+    p[0] = F32(start)
+    den = F32(F32(count) - F32(1.0))
+    for i in range(1, count + 1):
+        x = F32(F32(F32(i) - F32(1.0)) / den)
+        d[i] = F32(F32(d0) * F32(F32(1) - F32(F32(x ** F32(1.5)) * F32(0.8))))
+        p[i] = F32(p[i - 1] + d[i])
+    return p, d
+
+
+def symmetric_stretched(n, start, lo=None, hi=None, tol=None):
+    """Spacings of a spectral axis of n (even, >= 4) cells refined towards
+    zero and mirrored about it (gm1.f90:45-47): d0 makes the centre fall on
+    the middle face, p(n/2) + d(n/2) = 0, starting from p(0) = start.  The
+    bisection tolerance defaults to 1e-8 of the half span (the reference's
+    1e-8 for its span of 1)."""
+    if n < 4 or n % 2:
+        raise GridError("symmetric stretched axis needs an even n >= 4, got %d" % n)
+    half = n // 2
+
+    def closure(d0):
+        p, d = stretched_half(d0, start, half)
+        return F32(p[half] + d[half])
+
+    span = abs(float(start))
+    tol = 1e-8 * span if tol is None else tol
+    lo = span / (100.0 * half) if lo is None else lo
+    hi = 4.0 * span / half if hi is None else hi
+    d0 = bisect(closure, lo, hi, tol)
+    _, d = stretched_half(d0, start, half)
+    first = d[1:half + 1]
+    return np.concatenate([first, first[::-1]]).astype(np.float64)
+
+
+def bottom_refined(nz, Lz, lo=None, hi=None, tol=1e-8):
+    """z spacings of nz cells decreasing upward over a depth Lz (brava.f90
+    zgrid / zfunc): z(0) = -Lz - dz0/2 and dz0 makes the last centre fall on
+    z = 0, z(nz) + dz(nz)/2 = 0."""
+    Lz32 = F32(Lz)
+
+    def positions(dz0):
+        return stretched_half(dz0, F32(-Lz32 - F32(F32(dz0) / F32(2))), nz)
+
+    def closure(dz0):
+        p, d = positions(dz0)
+        return F32(p[nz] + F32(d[nz] / F32(2.0)))
+
+    lo = float(Lz) / nz / 10.0 if lo is None else lo
+    hi = float(Lz) if hi is None else hi
+    dz0 = bisect(closure, lo, hi, tol)
+    _, d = positions(dz0)
+    return d[1:].astype(np.float64)
+
+
 def calc_grid(n, d_interior, fixed=(0.0, 0.0, 0.0)):
     """Build padded grids for the six axes.
 

@@ -34,6 +34,9 @@ CASES = {
     "column_1d": lambda: configs.column_1d(fac=1),
     "section_2d": lambda: configs.section_2d(fac=0.5),
     "packet_small": lambda: configs.packet_small(),
+    "stretched": lambda: configs.stretched_mini(),
+    "stretched_open": lambda: configs.stretched_mini(n=(8, 8, 6, 4, 6, 4), upper=False, lower=False),
+    "gm_column": lambda: configs.gm_column(),
 }
 
 VEL = ("xdot", "ydot", "zdot", "kdot", "ldot", "mdot")
@@ -261,6 +264,28 @@ def test_fp32_form_against_fp64_oracle(variant):
         assert l2 <= 1e-5
         assert linf <= 1e-4
         assert drift <= 1e-6
+    finally:
+        m.close()
+
+
+@pytest.mark.parametrize("variant", ["tma", "group", "w2z", "w3", "w6", "w2d"])
+def test_fp32_stretched_against_fp64_oracle(variant):
+    """binary32 form on non-uniform grids (per-cell 1/d and dt/2d tables):
+    error after 100 steps of the stretched all-axes case, 8x8 planes and 256
+    threads so that every listed kernel takes it."""
+    exp = configs.stretched_mini(n=(8, 8, 8, 6, 6, 8))
+    m = configs.build_model(exp, "fp32")
+    m.set_tuning(variant, 8, 256)
+    o = build_oracle(exp)
+    sl = interior(exp.n)
+    try:
+        m.integrate(100)
+        o.integrate(100)
+        m.get_state()
+        ref, got = o.E[sl], m.E[sl]
+        l2 = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        assert l2 <= 1e-5, l2
+        assert max_rel(got, ref) <= 1e-4
     finally:
         m.close()
 
