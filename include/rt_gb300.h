@@ -168,6 +168,12 @@ int rt_get_state_interior(rt_handle* h, void* E);
 int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int, double* diss_ks,
                 double* diss_ke, double* diss_ls, double* diss_le, double* diss_ms,
                 double* diss_me);
+/* The module arrays dE and meanfl that the last step left behind
+ * (integrate.f90:202-262; dE after the mean-flow term), recomputed on the
+ * device from the state that step started from: padded 6D host arrays, the
+ * interior is written.  With E they form the restart record
+ * (restart.f90:15-18).  Needs a step since rt_set_state. */
+int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
 
 /* Schedule of the step kernel (no effect on results).  variant: 2 = plane
  * tiled with bulk-copy (TMA) staging of the E planes (default; used when a

@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libraytracer_gb300.so")
 
 RT_OK = 0
+RT_ERR_ARG, RT_ERR_NOMEM, RT_ERR_CUDA, RT_ERR_GRID, RT_ERR_STATE = -1, -2, -3, -4, -5
 RT_FP64 = 0
 RT_FP32 = 1
 
@@ -58,6 +59,7 @@ SIGNATURES = {
     "rt_get_state": (ctypes.c_int, [_P, _D]),
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_forcing": (ctypes.c_int, [_P, ctypes.c_int, _D]),
+    "rt_get_tendency": (ctypes.c_int, [_P, _D, _D]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_state_interior": (ctypes.c_int, [_P, _P]),
     "rt_get_state_interior": (ctypes.c_int, [_P, _P]),

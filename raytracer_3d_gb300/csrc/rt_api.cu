@@ -1274,6 +1274,45 @@ int rt_diagnose(rt_handle* h, rt_budget* o, double* E_int, double* meanfl_int, d
   return RT_OK;
 }
 
+int rt_get_tendency(rt_handle* h, double* dE, double* meanfl) {
+  if (!h) return RT_ERR_ARG;
+  if (!dE || !meanfl) return fail(h, RT_ERR_ARG, "rt_get_tendency: NULL array");
+  if (!h->have_state || h->steps_since_set < 1)
+    return fail(h, RT_ERR_STATE, "rt_get_tendency: needs a step since rt_set_state");
+  const Dims& d = h->d;
+  const int prev = 1 - h->cur;  // the state the last step started from
+  void* dev[2] = {nullptr, nullptr};
+  int rc = RT_OK;
+  std::vector<double> buf;
+  double* outs[2] = {dE, meanfl};
+  cudaError_t e;
+  for (int k = 0; k < 2 && !rc; k++) rc = tmp_alloc(h, &dev[k], (size_t)d.ncell * sizeof(double));
+  if (rc) goto cleanup;
+  if (h->p.precision == RT_FP64)
+    e = launch_tendency<double>(make_step_args<double>(h, prev), (double*)dev[0], (double*)dev[1], h->st);
+  else
+    e = launch_tendency<float>(make_step_args<float>(h, prev), (double*)dev[0], (double*)dev[1], h->st);
+  h->launches += 1;
+  if (e != cudaSuccess) {
+    rc = fail(h, RT_ERR_CUDA, "tendency launch: %s", cudaGetErrorString(e));
+    goto cleanup;
+  }
+  buf.resize((size_t)d.ncell);
+  for (int k = 0; k < 2; k++) {
+    e = cudaMemcpyAsync(buf.data(), dev[k], buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) {
+      rc = fail(h, RT_ERR_CUDA, "rt_get_tendency: %s", cudaGetErrorString(e));
+      goto cleanup;
+    }
+    scatter_interior(d, buf.data(), outs[k]);
+  }
+cleanup:
+  for (void* p : dev)
+    if (p) cudaFreeAsync(p, h->st);
+  return rc;
+}
+
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
   if (!h) return RT_ERR_ARG;
   if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA &&

@@ -830,4 +830,29 @@ template cudaError_t launch_diag<double>(const StepArgs<double>&, const double*,
 template cudaError_t launch_diag<float>(const StepArgs<float>&, const float*, double*, double*,
                                         double*, cudaStream_t);
 
+// the module arrays dE and meanfl that integrate leaves behind
+// (integrate.f90:202-262): per cell of the state A.E, dE after the mean-flow
+// term and meanfl, widened to binary64; unpadded, x fastest
+template <class T>
+__global__ void __launch_bounds__(256) tendency_kernel(StepArgs<T> A, double* dE, double* meanfl) {
+  const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v3 >= A.d.nvol3) return;
+  for (long long sp = blockIdx.y; sp < A.d.nspec; sp += gridDim.y) {
+    int c[6];
+    decode(A.d, v3, sp, c);
+    const long long p = v3 + sp * A.d.nvol3;
+    const CellTerms<T> t = cell_terms<T>(A, p, c, A.E[p]);
+    dE[p] = (double)tsub<T>(t.dE, t.meanfl);
+    meanfl[p] = (double)t.meanfl;
+  }
+}
+
+template <class T>
+cudaError_t launch_tendency(const StepArgs<T>& A, double* dE, double* meanfl, cudaStream_t st) {
+  tendency_kernel<T><<<cell_grid(A.d, 256), 256, 0, st>>>(A, dE, meanfl);
+  return cudaGetLastError();
+}
+template cudaError_t launch_tendency<double>(const StepArgs<double>&, double*, double*, cudaStream_t);
+template cudaError_t launch_tendency<float>(const StepArgs<float>&, double*, double*, cudaStream_t);
+
 }  // namespace rt

@@ -143,6 +143,10 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
 template <class T>
 cudaError_t launch_forcing(T* E, const double* F, const T* zdot, const Dims& d, double dt, double dz, int kind,
                            cudaStream_t st);
+// dE (after the mean-flow term) and meanfl of every cell of the state A.E,
+// as binary64 unpadded fields (rt_kernels.cu)
+template <class T>
+cudaError_t launch_tendency(const StepArgs<T>& A, double* dE, double* meanfl, cudaStream_t st);
 DiagSizes diag_sizes(const Dims& d);
 template <class T>
 cudaError_t launch_diag(const StepArgs<T>& A, const T* Ecur, double* scratch, double* vol3,

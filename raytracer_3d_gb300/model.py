@@ -161,6 +161,17 @@ class Model:
         self._check(self._lib.rt_get_state(self._h, _lib.dptr(self.E)), "rt_get_state")
         return self.E
 
+    def get_tendency(self):
+        """dE (after the mean-flow term) and meanfl of the last step, as
+        padded 6D arrays (rt_get_tendency); zeros before the first step, as
+        the reference allocates them."""
+        dE, mfl = zeros_padded(self.n), zeros_padded(self.n)
+        rc = self._lib.rt_get_tendency(self._h, _lib.dptr(dE), _lib.dptr(mfl))
+        if rc == _lib.RT_ERR_STATE and self.itt == 0:
+            return dE, mfl
+        self._check(rc, "rt_get_tendency")
+        return dE, mfl
+
     # ---- bottom forcing (set_forcing, main.f90:69) ------------------------------
     FORCING = {"none": _lib.RT_FORCING_NONE, "flux": _lib.RT_FORCING_FLUX, "relax": _lib.RT_FORCING_RELAX}
 
