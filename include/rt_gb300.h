@@ -268,6 +268,16 @@ int rt_batch_stream(rt_batch* b, void** stream);
 long long rt_batch_launch_count(const rt_batch* b);
 long long rt_batch_cells(const rt_batch* b);
 
+/* Failure-detection self-test of the bounded device waits.  Every wait of
+ * the step kernels on an mbarrier gives up after a fixed number of polls,
+ * raises a status flag that the next synchronising call turns into
+ * RT_ERR_CUDA ("a device-side wait timed out"), lets copies in flight land
+ * and returns, so the context stays usable.  This call runs one CTA whose
+ * waits can never complete, through the same wait code with a short limit,
+ * and reports *status (the raised flag, 1 expected) and *completed (1 if a
+ * wait completed, 0 expected).  It touches no handle. */
+int rt_selftest_wait_timeout(int* status, int* completed);
+
 #ifdef __cplusplus
 }
 #endif

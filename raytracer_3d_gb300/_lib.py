@@ -60,6 +60,7 @@ SIGNATURES = {
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_forcing": (ctypes.c_int, [_P, ctypes.c_int, _D]),
     "rt_get_tendency": (ctypes.c_int, [_P, _D, _D]),
+    "rt_selftest_wait_timeout": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_state_interior": (ctypes.c_int, [_P, _P]),
     "rt_get_state_interior": (ctypes.c_int, [_P, _P]),

@@ -745,6 +745,25 @@ long long rt_batch_launch_count(const rt_batch* b) { return b ? b->launches : 0;
 long long rt_batch_cells(const rt_batch* b) { return b ? b->cells : 0; }
 
 
+int rt_selftest_wait_timeout(int* status, int* completed) {
+  if (!status || !completed) return fail(nullptr, RT_ERR_ARG, "rt_selftest_wait_timeout: NULL argument");
+  int* dev = nullptr;
+  cudaError_t e = cudaMalloc(&dev, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dev, 0, 2 * sizeof(int));
+  if (e == cudaSuccess) e = launch_wait_probe(dev, dev + 1, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int host[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(host, dev, sizeof(host), cudaMemcpyDeviceToHost);
+  if (dev) cudaFree(dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, RT_ERR_CUDA, "rt_selftest_wait_timeout: %s", cudaGetErrorString(e));
+  }
+  *status = host[0];
+  *completed = host[1];
+  return RT_OK;
+}
+
 const char* rt_version(void) { return "raytracer_gb300 0.1 (sm_103a)"; }
 
 const char* rt_last_error(const rt_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }

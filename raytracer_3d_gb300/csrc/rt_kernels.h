@@ -137,6 +137,9 @@ cudaError_t launch_batch_w6(const void* members, const long long* first, int nme
 // rt_persist.cu, rt_persist_w2.cu, rt_persist_ws.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);
+// failure-detection self-test of the bounded waits (rt_persist.cu): one CTA
+// whose waits cannot complete; raises *status, leaves *completed at 0
+cudaError_t launch_wait_probe(int* status, int* completed, cudaStream_t st);
 // set_forcing on the bottom z plane, in place on E (rt_forcing.cu); kind
 // RT_FORCING_FLUX or RT_FORCING_RELAX of rt_gb300.h, F the interior 5D
 // forcing field (x,y,k,l,m), zdot the z face velocities (RELAX only)

@@ -164,6 +164,33 @@ cudaError_t launch_batch_w3(const void* members, const long long* first, int nme
   return launch_bw3_nt<512>(members, first, nmem, R, ns, stage_floats, grid, st);
 }
 
+// failure-detection self-test: one CTA of two warps waits on mbarriers that
+// nothing completes, through the same bounded-wait helpers the step kernels
+// use (a warp wait as the persistent consumers and producer do, a per-thread
+// wait as the plane kernels do), with a short poll limit.  Nothing is copied,
+// so no transfer is in flight when the waits give up.
+#define RT_PROBE_LIMIT (1u << 12)
+
+namespace {
+__global__ void __launch_bounds__(64) wait_probe_kernel(int* status, int* completed) {
+  __shared__ uint64_t bar[2];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool a = warp_wait<RT_PROBE_LIMIT>(&bar[0], 0, status);
+  const bool b = mbar_wait_bounded<RT_PROBE_LIMIT>(&bar[1], 0, status);
+  if (a || b) atomicOr(completed, 1);
+}
+}  // namespace
+
+cudaError_t launch_wait_probe(int* status, int* completed, cudaStream_t st) {
+  wait_probe_kernel<<<1, 64, 0, st>>>(status, completed);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done) {
   done = false;
   if (tn.variant == RT_VARIANT_W6 && w6_slices(A.d, tn.threads) > 0) {

@@ -56,12 +56,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
-// bounded wait; returns false (and raises the status flag) on timeout
+// bounded wait; returns false (and raises the status flag) on timeout.
+// LIMIT polls (the failure-detection self-test uses a short one)
+template <uint32_t LIMIT = RT_WAIT_LIMIT>
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t it = 0; it < RT_WAIT_LIMIT; it++)
+  for (uint32_t it = 0; it < LIMIT; it++)
     if (mbar_try_wait(bar, parity)) return true;
   if (threadIdx.x == 0) atomicOr(status, 1);
-  for (uint32_t it = 0; it < RT_WAIT_LIMIT; it++)  // let copies in flight land
+  for (uint32_t it = 0; it < LIMIT; it++)  // let copies in flight land
     if (mbar_try_wait(bar, parity)) break;
   return false;
 }

@@ -53,8 +53,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 // bounded wait from any thread; raises status bit 0 on timeout
+template <uint32_t LIMIT = RT_WAIT_LIMIT>
 __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t it = 0; it < RT_WAIT_LIMIT; it++)
+  for (uint32_t it = 0; it < LIMIT; it++)
     if (mbar_try_wait(bar, parity)) return true;
   atomicOr(status, 1);
   return false;
@@ -62,9 +63,10 @@ __device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, int* sta
 
 // bounded wait of a whole warp: lane 0 polls, the result is broadcast, and
 // __syncwarp orders the other lanes' later accesses after lane 0's acquire
+template <uint32_t LIMIT = RT_WAIT_LIMIT>
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* status) {
   bool ok = true;
-  if ((threadIdx.x & 31) == 0) ok = ws_wait(bar, parity, status);
+  if ((threadIdx.x & 31) == 0) ok = ws_wait<LIMIT>(bar, parity, status);
   ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
   __syncwarp();
   return ok;

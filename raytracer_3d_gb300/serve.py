@@ -36,6 +36,10 @@ class Request:
     admitted: Optional[float] = None
     finished: Optional[float] = None
     result: Any = None
+    cancel_at: Optional[float] = None   # the client gives up at this time (s after the start)
+    status: str = "queued"              # queued, running, done, cancelled, failed
+    error: Optional[str] = None
+    ended: Optional[float] = None       # when a cancelled or failed request left
 
     @property
     def latency(self):
@@ -82,7 +86,7 @@ class ServeReport:
     timeline: list = field(default_factory=list)
 
     def percentile(self, q):
-        lat = sorted(r.latency for r in self.requests if r.latency is not None)
+        lat = sorted(r.latency for r in self.requests if r.status == "done")
         if not lat:
             return None
         k = max(0, min(len(lat) - 1, int(math.ceil(q / 100.0 * len(lat))) - 1))
@@ -90,7 +94,9 @@ class ServeReport:
 
     def summary(self):
         return {"requests": len(self.requests),
-                "completed": sum(r.finished is not None for r in self.requests),
+                "completed": sum(r.status == "done" for r in self.requests),
+                "cancelled": sum(r.status == "cancelled" for r in self.requests),
+                "failed": sum(r.status == "failed" for r in self.requests),
                 "p50_s": self.percentile(50), "p99_s": self.percentile(99),
                 "makespan_s": self.makespan,
                 "cell_updates_per_s": self.cell_updates / self.makespan if self.makespan > 0 else None,
@@ -101,7 +107,14 @@ class Server:
     """Continuous-batching request loop.  With an executor whose
     `overlap_setup` is true, set-up of admitted requests (`admit_async`) runs
     in a background thread pool while chunks run on the GPU; new members join
-    at the next chunk boundary once their set-up has finished."""
+    at the next chunk boundary once their set-up has finished.
+
+    One request's trouble does not reach the others: a set-up or a retire
+    that raises marks that request "failed" (with the error) and returns its
+    memory to the budget; a request whose cancel_at has passed is dropped at
+    the next chunk boundary ("cancelled"), before admission, during set-up
+    or while running, and its member is discarded.  A failing chunk (the
+    batched launch itself) ends the run with the error."""
 
     def __init__(self, executor, budget_bytes=120e9, chunk_max=50, max_members=64, setup_workers=2):
         self.ex = executor
@@ -136,6 +149,10 @@ class Server:
                 while (qi < len(queue) and queue[qi].arrival <= now
                        and len(active) + len(pending) < self.max_members):
                     r = queue[qi]
+                    if _gave_up(r, now):
+                        _end(r, "cancelled", ex.now() - t0)
+                        qi += 1
+                        continue
                     need_res, need_tmp = ex.footprint(r)
                     if need_res + need_tmp > self.budget:
                         raise ValueError("request %d needs %.3g B, more than the whole budget"
@@ -143,24 +160,45 @@ class Server:
                     if used + transient + need_res + need_tmp > self.budget:
                         break                                    # wait for memory to free up
                     r.admitted = ex.now() - t0
+                    r.status = "running"
                     used += need_res
                     if asynchronous:
                         transient += need_tmp
                         pending.append([r, pool.submit(ex.admit_async, r)])
                     else:
-                        member = ex.admit(r)
-                        active.append([r, member, r.steps])
+                        try:
+                            member = ex.admit(r)
+                        except Exception as e:                   # this request only
+                            used -= need_res
+                            _end(r, "failed", ex.now() - t0, e)
+                        else:
+                            active.append([r, member, r.steps])
                     peak = max(peak, used + transient + (0 if asynchronous else need_tmp))
                     qi += 1
-                # ---- set-ups that finished join the batch ----
+                # ---- set-ups that finished join the batch (or fail alone) ----
                 still = []
                 for r, fut in pending:
                     if fut.done():
-                        active.append([r, fut.result(), r.steps])
                         transient -= ex.footprint(r)[1]
+                        try:
+                            member = fut.result()
+                        except Exception as e:
+                            used -= ex.footprint(r)[0]
+                            _end(r, "failed", ex.now() - t0, e)
+                            continue
+                        active.append([r, member, r.steps])
                     else:
                         still.append([r, fut])
                 pending = still
+                # ---- clients that gave up leave at this chunk boundary ----
+                gone = [a for a in active if _gave_up(a[0], now)]
+                if gone:
+                    ex.sync()
+                    for a in gone:
+                        _discard(ex, a[1])
+                        used -= ex.footprint(a[0])[0]
+                        _end(a[0], "cancelled", ex.now() - t0)
+                    active = [a for a in active if not _gave_up(a[0], now)]
                 backlog = sum(1 for r in queue[qi:] if r.arrival <= now)
                 backlog_max = max(backlog_max, backlog)
                 if not active:
@@ -182,16 +220,39 @@ class Server:
                     ex.sync()
                     for a in done:
                         r = a[0]
-                        r.result = ex.retire(a[1])
-                        r.finished = ex.now() - t0
                         used -= ex.footprint(r)[0]
+                        try:
+                            r.result = ex.retire(a[1])
+                        except Exception as e:                   # this request only
+                            _end(r, "failed", ex.now() - t0, e)
+                            continue
+                        r.finished = ex.now() - t0
+                        r.status = "done"
                     active = [a for a in active if a[2] > 0]
                 timeline.append((ex.now() - t0, len(active), used))
         finally:
             if pool is not None:
                 pool.shutdown(wait=True)
+        for r, fut in pending:          # only after an error: set-ups still in flight
+            if fut.done() and fut.exception() is None:
+                _discard(ex, fut.result())
         makespan = ex.now() - t0
         return ServeReport(queue, makespan, total, int(peak), chunks, backlog_max, timeline)
+
+
+def _gave_up(r, now):
+    return r.cancel_at is not None and r.cancel_at <= now
+
+
+def _end(r, status, t, err=None):
+    r.status = status
+    r.error = None if err is None else "%s: %s" % (type(err).__name__, err)
+    r.ended = t
+
+
+def _discard(ex, member):
+    """free a member without reading its result"""
+    getattr(ex, "discard", ex.retire)(member)
 
 
 class GpuExecutor:
@@ -265,10 +326,15 @@ class GpuExecutor:
 
     def retire(self, member):
         t0 = time.perf_counter()
-        E = member.get_state()   # interior, in the member's precision
-        member.close()
+        try:
+            E = member.get_state()   # interior, in the member's precision
+        finally:
+            member.close()
         self.times["retire"] += time.perf_counter() - t0
         return E
+
+    def discard(self, member):
+        member.close()
 
     def close(self):
         if self._batch is not None:
@@ -294,13 +360,16 @@ class FakeExecutor:
     of n steps over members costs n * (launch + sum(cells) / rate) seconds,
     admission costs setup_s; results record which steps each member saw."""
 
-    def __init__(self, rate=1e10, launch=1e-5, setup_s=1e-3, bpc=(36.0, 72.0)):
+    def __init__(self, rate=1e10, launch=1e-5, setup_s=1e-3, bpc=(36.0, 72.0), fail_admit=(), fail_retire=()):
         self.t = 0.0
         self.rate = rate
         self.launch = launch
         self.setup_s = setup_s
         self.bpc = bpc
         self.log = []
+        self.fail_admit = set(fail_admit)     # request ids whose set-up raises
+        self.fail_retire = set(fail_retire)   # request ids whose result read raises
+        self.discarded = []
 
     def now(self):
         return self.t
@@ -313,6 +382,8 @@ class FakeExecutor:
 
     def admit(self, r):
         self.t += self.setup_s
+        if r.rid in self.fail_admit:
+            raise RuntimeError("injected set-up failure of request %d" % r.rid)
         return {"rid": r.rid, "steps": 0, "cells": r.cells}
 
     def step(self, members, n):
@@ -325,4 +396,9 @@ class FakeExecutor:
         pass
 
     def retire(self, member):
+        if member["rid"] in self.fail_retire:
+            raise RuntimeError("injected result failure of request %d" % member["rid"])
         return member["steps"]
+
+    def discard(self, member):
+        self.discarded.append(member["rid"])

@@ -60,3 +60,66 @@ def test_percentiles_and_poisson_generator():
     s = rep.summary()
     assert s["completed"] == 40
     assert s["p50_s"] <= s["p99_s"]
+
+
+# ---- failure isolation: injected on the host, no GPU involved ----
+def test_failed_setup_leaves_the_others_exact():
+    reqs = _reqs([(1000, 40, 0.0), (2000, 30, 0.0), (500, 25, 0.001), (800, 60, 0.002)])
+    ex = FakeExecutor(rate=1e6, fail_admit={1})
+    rep = Server(ex, budget_bytes=1e9, chunk_max=10).run(reqs)
+    assert reqs[1].status == "failed" and "injected set-up failure" in reqs[1].error
+    for r in (reqs[0], reqs[2], reqs[3]):
+        assert r.status == "done" and r.result == r.steps
+    assert all(1 not in ids for _, ids, _ in ex.log)
+    s = rep.summary()
+    assert (s["completed"], s["failed"], s["cancelled"]) == (3, 1, 0)
+    assert rep.cell_updates == sum(r.cells * r.steps for r in reqs if r.status == "done")
+
+
+def test_failed_setup_returns_its_memory():
+    # the budget holds one request; the first fails, the second must still run
+    reqs = _reqs([(1000, 10, 0.0), (1000, 10, 0.0)])
+    budget = 36 * 1000 + 72 * 1000 + 1
+    rep = Server(FakeExecutor(rate=1e6, fail_admit={0}), budget_bytes=budget, chunk_max=5).run(reqs)
+    assert reqs[0].status == "failed" and reqs[1].status == "done" and reqs[1].result == 10
+    assert rep.peak_bytes <= budget
+
+
+def test_failed_result_read_is_contained():
+    reqs = _reqs([(1000, 20, 0.0), (1000, 20, 0.0), (1000, 50, 0.0)])
+    ex = FakeExecutor(rate=1e6, fail_retire={0})
+    Server(ex, budget_bytes=1e9, chunk_max=10).run(reqs)
+    assert reqs[0].status == "failed" and reqs[0].result is None
+    assert reqs[1].result == 20 and reqs[2].result == 50
+
+
+@pytest.mark.parametrize("when", ["queued", "running"])
+def test_cancelled_request_leaves_without_perturbing_the_others(when):
+    # 1000 cells at 1e6 cells/s: 1 ms per step per member
+    reqs = _reqs([(1000, 100, 0.0), (1000, 100, 0.0), (1000, 30, 0.0), (1000, 80, 0.05)])
+    if when == "queued":
+        reqs[3].cancel_at = 0.01          # before it arrives
+    else:
+        reqs[1].cancel_at = 0.03          # mid-flight
+    ex = FakeExecutor(rate=1e6)
+    rep = Server(ex, budget_bytes=1e9, chunk_max=10).run(reqs)
+    gone = reqs[3] if when == "queued" else reqs[1]
+    assert gone.status == "cancelled" and gone.result is None and gone.finished is None
+    for r in reqs:
+        if r is not gone:
+            assert r.status == "done" and r.result == r.steps
+    if when == "running":
+        assert ex.discarded == [1]
+        last = max(t for t, ids, _ in ex.log if 1 in ids)
+        assert last <= 0.03 + 0.05        # left at a chunk boundary after cancel_at
+    assert rep.summary()["cancelled"] == 1
+
+
+def test_cancellation_frees_budget_for_the_queue():
+    # budget for one request at a time; cancelling the first lets the second start early
+    reqs = _reqs([(1000, 1000, 0.0), (1000, 10, 0.0)])
+    reqs[0].cancel_at = 0.02
+    budget = 36 * 1000 + 72 * 1000 + 1
+    Server(FakeExecutor(rate=1e6), budget_bytes=budget, chunk_max=10).run(reqs)
+    assert reqs[0].status == "cancelled"
+    assert reqs[1].status == "done" and reqs[1].admitted < 0.1
