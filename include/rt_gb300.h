@@ -268,6 +268,19 @@ int rt_batch_stream(rt_batch* b, void** stream);
 long long rt_batch_launch_count(const rt_batch* b);
 long long rt_batch_cells(const rt_batch* b);
 
+/* Phase timers, the GPU counterpart of the reference's tic/toc counters
+ * (timing_module.f90:34-75, printed at main.f90:86-101): rt_tic / rt_toc
+ * record CUDA events on the handle's stream around the named phase (so the
+ * device time of the work queued in between is measured, without a
+ * synchronisation); rt_timing_secs waits for the recorded events and
+ * returns the accumulated seconds and the number of tic/toc pairs.  A toc
+ * without its tic, or a second tic, is RT_ERR_STATE; an unknown name reads
+ * as 0 s.  The fused step has no separate fluxes / bc exchange / reflection
+ * / time tendency phases: they are all inside 'integrate'. */
+int rt_tic(rt_handle* h, const char* name);
+int rt_toc(rt_handle* h, const char* name);
+int rt_timing_secs(rt_handle* h, const char* name, double* secs, long long* calls);
+
 /* Failure-detection self-test of the bounded device waits.  Every wait of
  * the step kernels on an mbarrier gives up after a fixed number of polls,
  * raises a status flag that the next synchronising call turns into

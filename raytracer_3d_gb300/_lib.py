@@ -60,6 +60,9 @@ SIGNATURES = {
     "rt_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_forcing": (ctypes.c_int, [_P, ctypes.c_int, _D]),
     "rt_get_tendency": (ctypes.c_int, [_P, _D, _D]),
+    "rt_tic": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "rt_toc": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "rt_timing_secs": (ctypes.c_int, [_P, ctypes.c_char_p, _D, ctypes.POINTER(ctypes.c_longlong)]),
     "rt_selftest_wait_timeout": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_state_interior": (ctypes.c_int, [_P, _P]),

@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -65,6 +66,15 @@ struct rt_handle {
   long long launches = 0;
   long long bytes = 0;
   cudaEvent_t ev = nullptr;     // orders this handle's stream against a batch stream
+  // named phase timers (rt_tic / rt_toc): event pairs on the handle's stream,
+  // resolved when rt_timing_secs reads them
+  struct Timer {
+    double secs = 0.0;
+    long long calls = 0;
+    cudaEvent_t open = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
+  };
+  std::map<std::string, Timer> timers;
   std::string err;
 };
 
@@ -873,6 +883,13 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->result);
   cudaFree(h->status);
   cudaFree(h->force);
+  for (auto& kv : h->timers) {
+    if (kv.second.open) cudaEventDestroy(kv.second.open);
+    for (auto& pr : kv.second.pairs) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  }
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->ev) cudaEventDestroy(h->ev);
   if (h->st) cudaStreamDestroy(h->st);
@@ -1330,6 +1347,69 @@ cleanup:
   for (void* p : dev)
     if (p) cudaFreeAsync(p, h->st);
   return rc;
+}
+
+int rt_tic(rt_handle* h, const char* name) {
+  if (!h) return RT_ERR_ARG;
+  if (!name || !*name) return fail(h, RT_ERR_ARG, "rt_tic: empty timer name");
+  rt_handle::Timer& t = h->timers[name];
+  if (t.open) return fail(h, RT_ERR_STATE, "rt_tic: timer '%s' is already running", name);
+  cudaEvent_t e;
+  CUDA_TRY(h, cudaEventCreate(&e));
+  const cudaError_t r = cudaEventRecord(e, h->st);
+  if (r != cudaSuccess) {
+    cudaEventDestroy(e);
+    return fail(h, RT_ERR_CUDA, "rt_tic: %s", cudaGetErrorString(r));
+  }
+  t.open = e;
+  return RT_OK;
+}
+
+int rt_toc(rt_handle* h, const char* name) {
+  if (!h) return RT_ERR_ARG;
+  if (!name) return fail(h, RT_ERR_ARG, "rt_toc: NULL timer name");
+  auto it = h->timers.find(name);
+  if (it == h->timers.end() || !it->second.open)
+    return fail(h, RT_ERR_STATE, "rt_toc: timer '%s' was not started", name);
+  cudaEvent_t e;
+  CUDA_TRY(h, cudaEventCreate(&e));
+  const cudaError_t r = cudaEventRecord(e, h->st);
+  if (r != cudaSuccess) {
+    cudaEventDestroy(e);
+    return fail(h, RT_ERR_CUDA, "rt_toc: %s", cudaGetErrorString(r));
+  }
+  it->second.pairs.emplace_back(it->second.open, e);
+  it->second.open = nullptr;
+  it->second.calls += 1;
+  return RT_OK;
+}
+
+int rt_timing_secs(rt_handle* h, const char* name, double* secs, long long* calls) {
+  if (!h) return RT_ERR_ARG;
+  if (!name || !secs) return fail(h, RT_ERR_ARG, "rt_timing_secs: NULL argument");
+  auto it = h->timers.find(name);
+  if (it == h->timers.end()) {
+    *secs = 0.0;
+    if (calls) *calls = 0;
+    return RT_OK;
+  }
+  rt_handle::Timer& t = it->second;
+  size_t used = 0;  // pairs folded into secs and destroyed
+  cudaError_t e = cudaSuccess;
+  for (; used < t.pairs.size(); used++) {
+    float ms = 0.f;
+    e = cudaEventSynchronize(t.pairs[used].second);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t.pairs[used].first, t.pairs[used].second);
+    if (e != cudaSuccess) break;
+    t.secs += ms * 1e-3;
+    cudaEventDestroy(t.pairs[used].first);
+    cudaEventDestroy(t.pairs[used].second);
+  }
+  t.pairs.erase(t.pairs.begin(), t.pairs.begin() + (long)used);
+  if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "rt_timing_secs: %s", cudaGetErrorString(e));
+  *secs = t.secs;
+  if (calls) *calls = t.calls;
+  return RT_OK;
 }
 
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {

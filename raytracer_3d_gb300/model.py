@@ -172,6 +172,44 @@ class Model:
         self._check(rc, "rt_get_tendency")
         return dE, mfl
 
+    # ---- phase timers (timing_module.f90 tic / toc) -----------------------------
+    def tic(self, name):
+        """start the named phase timer (a CUDA event on the handle's stream)"""
+        self._check(self._lib.rt_tic(self._h, name.encode()), "rt_tic")
+
+    def toc(self, name):
+        self._check(self._lib.rt_toc(self._h, name.encode()), "rt_toc")
+
+    def timing_secs(self, name):
+        """(device seconds, tic/toc pairs) accumulated for the named phase"""
+        secs, calls = ctypes.c_double(), ctypes.c_longlong()
+        self._check(self._lib.rt_timing_secs(self._h, name.encode(), ctypes.byref(secs), ctypes.byref(calls)),
+                    "rt_timing_secs")
+        return secs.value, calls.value
+
+    def timed(self, name):
+        """context manager: tic on entry, toc on exit"""
+        model = self
+
+        class _Phase:
+            def __enter__(self):
+                model.tic(name)
+                return model
+
+            def __exit__(self, *exc):
+                model.toc(name)
+                return False
+        return _Phase()
+
+    def timing_summary(self, names=("main loop", "integrate", "diag")):
+        """the reference's end-of-run summary (main.f90:86-101) for the
+        named phases, as text"""
+        lines = []
+        for n in names:
+            secs, calls = self.timing_secs(n)
+            lines.append("%-25s = %12.4f s  (%d calls)" % (n, secs, calls))
+        return "\n".join(lines)
+
     # ---- bottom forcing (set_forcing, main.f90:69) ------------------------------
     FORCING = {"none": _lib.RT_FORCING_NONE, "flux": _lib.RT_FORCING_FLUX, "relax": _lib.RT_FORCING_RELAX}
 

@@ -65,3 +65,12 @@ def test_argument_validation_without_gpu(lib):
 
 def test_version_string(lib):
     assert b"sm_103a" in lib.rt_version()
+
+
+def test_timers_and_selftest_reject_null_arguments(lib):
+    assert lib.rt_tic(None, b"integrate") == -1
+    assert lib.rt_toc(None, b"integrate") == -1
+    secs = ctypes.c_double()
+    assert lib.rt_timing_secs(None, b"integrate", ctypes.byref(secs), None) == -1
+    assert lib.rt_selftest_wait_timeout(None, None) == -1
+    assert lib.rt_get_tendency(None, None, None) == -1
