@@ -178,6 +178,7 @@ def time_steps(model, steps):
 
 FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w2d", "w6") for t in (128, 256, 512) for b in (4, 8)
                     for s in (0, 1)]
+                   + [("w2", b, t, s) for t in (256, 512) for b in (4, 8) for s in (0, 1)]
                    + [(v, b, t, s) for v in ("pipe", "tma") for t in (256, 512, 1024) for b in (4, 8)
                       for s in (0, 1)])
 
