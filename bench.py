@@ -183,7 +183,12 @@ FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w2d", "w6") for t in (1
                       for s in (0, 1)])
 
 
-def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False):
+# binary64: the fused plane kernel, or the two-pass step that evaluates every
+# face flux once (FP64-pipe bound either way); dry steps pick the faster
+FP64_CANDIDATES = [("tma", 8, 256, 0), ("split", 8, 256, 0)]
+
+
+def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False, candidates=None):
     import numpy as np
     import torch
     from raytracer_3d_gb300 import configs
@@ -193,7 +198,7 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
     table = None
     if tune:
         from raytracer_3d_gb300.autotune import tune_model
-        tuned, table = tune_model(m, candidates=FP32_CANDIDATES, reps=2, use_cache=False)
+        tuned, table = tune_model(m, candidates=candidates or FP32_CANDIDATES, reps=2, use_cache=False)
     elif sched:
         m.set_tuning(*sched)
     cells = exp.cells
@@ -304,10 +309,10 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
                                    "p50_s": sb["p50_s"], "p99_s": sb["p99_s"]}}
 
 
-def roofline(precision, cells, seconds_per_launch):
+def roofline(precision, cells, seconds_per_launch, traffic_key=None):
     peak, src = peaks()
     achieved = B_ALG[precision] * cells / seconds_per_launch / 1e9
-    tb = profile_traffic("step_%s" % precision)
+    tb = profile_traffic(traffic_key or "step_%s" % precision)
     return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src
             if src == "measured" else "fallback 6.8 TB/s",
@@ -342,7 +347,10 @@ def gpu_arm(args):
         return
     # the binary64 form is bound by the FP64 pipe; 256-thread CTAs keep its
     # registers unspilled (the flags set the fp32 schedule when --tune 0)
-    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, ("tma", 8, 256, 0))
+    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, FP64_CANDIDATES[0],
+                    tune=args.tune, candidates=FP64_CANDIDATES)
+    f64_sched = tuple(main["schedule"])
+    f64_split = f64_sched[0] == "split"
     forms = {}
     if not args.no_fp32:
         f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
@@ -364,9 +372,11 @@ def gpu_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded log-normal spectrum, analytic N(z), U(y,z))",
         "config": {"workload": "jet_large %d^3x%d^3 plain fp64, CFL 0.4 (dt=%%.6g s)" % (n[0], n[0]) % main["dt"],
-                   "cells": cells, "form": "fp64", "schedule": "tma band 8 threads 256 sweep 0", "l2": "state 8.6 GB per field >> L2; no flush needed",
+                   "cells": cells, "form": "fp64", "schedule": "%s band %d threads %d sweep %d" % f64_sched,
+                   "tuning_table_ms": main["tuning_table_ms"], "l2": "state 8.6 GB per field >> L2; no flush needed",
                    "parallelism": "replicas x%d" % world},
-        "roofline": roofline("fp64", cells, main["seconds"] / args.steps),
+        "roofline": roofline("fp64", cells, main["seconds"] / args.steps,
+                             "step_fp64_split" if f64_split else "step_fp64"),
         "clocks": main["clocks"],
         "gpu_launches": main["launches"],
     }

@@ -188,9 +188,12 @@ int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
  * CTA size 128, 256, 512 or 1024 (default 512; consumer threads of
  * variants 5 and 6: 128, 256 or 512).  Variants 7-14 are further forms
  * of the persistent binary32 kernel (raytracer_3d_gb300.model.Model.VARIANTS;
- * 8 = 2-wide cell blocks, 14 = the same walking whole z columns).  Shapes a variant cannot run fall
- * back to the next one that can.  Chosen by the autotuner
- * (raytracer_3d_gb300.autotune). */
+ * 8 = 2-wide cell blocks, 14 = the same walking whole z columns).
+ * 15 = binary64 in two passes: every face flux evaluated once into flux
+ * fields (allocated by this call: 48 bytes per cell plus the face-0
+ * planes), then divergence and update; the binary32 form treats it as 2.
+ * Shapes a variant cannot run fall back to the next one that can.  Chosen
+ * by the autotuner (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);
 /* Sweep order of the plane schedule: 0 = bands over m (default), 1 = bands
  * over l.  No effect on results. */

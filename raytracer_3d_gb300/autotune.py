@@ -82,7 +82,11 @@ def tune_model(model, candidates=None, reps=3, use_cache=True):
     lib = model._lib
     timed = _event_timer(model.stream())
     table = []
-    for cand in candidates or DEFAULT_CANDIDATES:
+    if candidates is None:
+        candidates = list(DEFAULT_CANDIDATES)
+        if model.precision == "fp64":       # the two-pass binary64 step (every face flux once)
+            candidates.append(("split", 8, 256, 0))
+    for cand in candidates:
         model.set_tuning(*cand)
         run = lambda k: model._check(lib.rt_step_dry(model.handle, k), "rt_step_dry")  # noqa: E731
         run(1)  # warm-up (shared-memory attribute, caches)

@@ -51,6 +51,7 @@ struct rt_handle {
   double* force = nullptr;      // its interior 5D field (x,y,k,l,m)
   long long force_gen = 0;      // changes with every rt_set_forcing
   double dzt1 = 0.0;            // dzt(1), the bottom cell's spacing
+  SplitFluxes split{};          // flux fields of the two-pass binary64 step (allocated on selection)
   double* scratch = nullptr;    // reductions
   long long scratch_len = 0;
   double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
@@ -224,6 +225,36 @@ static cudaError_t apply_forcing(rt_handle* h, int buf, cudaStream_t st) {
                                   h->forcing, st);
   return launch_forcing<float>((float*)h->E[buf], h->force, (const float*)h->vel[2], h->d, h->p.dt, dzt1,
                                h->forcing, st);
+}
+
+// one step of the handle from buffer src into 1 - src; returns the kernels launched
+static cudaError_t step_once(rt_handle* h, int src, int* nlaunch) {
+  if (h->p.precision == RT_FP64) {
+    // the two-pass step once its fields exist (rt_set_tuning allocates them;
+    // a field with no axis longer than one keeps the fused step)
+    bool split = false;
+    for (int a = 0; a < 6; a++) split = split || h->split.f[a] != nullptr;
+    if (h->tune.variant == RT_VARIANT_SPLIT && split) {
+      *nlaunch = 2;
+      return launch_step_split(make_step_args<double>(h, src), h->split, h->st);
+    }
+    *nlaunch = 1;
+    return launch_step<double>(make_step_args<double>(h, src), h->tune, h->st);
+  }
+  *nlaunch = 1;
+  return launch_step<float>(make_step_args<float>(h, src), h->tune, h->st);
+}
+
+// flux fields of the two-pass binary64 step, for the axes with n > 1
+static int ensure_split(rt_handle* h) {
+  const Dims& d = h->d;
+  for (int a = 0; a < 6; a++) {
+    if (d.n[a] <= 1 || h->split.f[a]) continue;
+    int rc = dev_alloc(h, (void**)&h->split.f[a], (size_t)d.ncell * sizeof(double));
+    if (!rc) rc = dev_alloc(h, (void**)&h->split.f0[a], (size_t)(d.ncell / d.n[a]) * sizeof(double));
+    if (rc) return rc;
+  }
+  return RT_OK;
 }
 
 // binary64 form: refresh the cached uCFL fields (after the coefficients or dt change)
@@ -883,6 +914,7 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->result);
   cudaFree(h->status);
   cudaFree(h->force);
+  for (int a = 0; a < 6; a++) { cudaFree(h->split.f[a]); cudaFree(h->split.f0[a]); }
   for (auto& kv : h->timers) {
     if (kv.second.open) cudaEventDestroy(kv.second.open);
     for (auto& pr : kv.second.pairs) {
@@ -1218,9 +1250,9 @@ int rt_integrate(rt_handle* h, int nsteps) {
       h->launches += 1;
       if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "forcing launch: %s", cudaGetErrorString(e));
     }
-    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->tune, h->st);
-    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->tune, h->st);
-    h->launches += 1;
+    int nl = 1;
+    e = step_once(h, h->cur, &nl);
+    h->launches += nl;
     if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     h->cur = 1 - h->cur;
     h->steps_since_set += 1;
@@ -1233,10 +1265,9 @@ int rt_step_dry(rt_handle* h, int nsteps) {
   if (nsteps < 0) return fail(h, RT_ERR_ARG, "rt_step_dry: nsteps < 0");
   if (!h->have_coeff || !h->have_state) return fail(h, RT_ERR_STATE, "rt_step_dry: no state");
   for (int t = 0; t < nsteps; t++) {
-    cudaError_t e;
-    if (h->p.precision == RT_FP64) e = launch_step<double>(make_step_args<double>(h, h->cur), h->tune, h->st);
-    else e = launch_step<float>(make_step_args<float>(h, h->cur), h->tune, h->st);
-    h->launches += 1;
+    int nl = 1;
+    const cudaError_t e = step_once(h, h->cur, &nl);
+    h->launches += nl;
     if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
   }
   // the other buffer now holds E after one step; the state itself is unchanged,
@@ -1418,11 +1449,16 @@ int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
       variant != RT_VARIANT_GROUP && variant != RT_VARIANT_PIPE && variant != RT_VARIANT_WS &&
       variant != RT_VARIANT_WSD && variant != RT_VARIANT_W2 && variant != RT_VARIANT_W2D &&
       variant != RT_VARIANT_W3 && variant != RT_VARIANT_W4 && variant != RT_VARIANT_W5 &&
-      variant != RT_VARIANT_W5H && variant != RT_VARIANT_W6 && variant != RT_VARIANT_W2Z)
+      variant != RT_VARIANT_W5H && variant != RT_VARIANT_W6 && variant != RT_VARIANT_W2Z &&
+      variant != RT_VARIANT_SPLIT)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
   if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: threads must be 128, 256, 512 or 1024");
+  if (variant == RT_VARIANT_SPLIT && h->p.precision == RT_FP64) {
+    const int rc = ensure_split(h);
+    if (rc) return rc;
+  }
   h->tune.variant = variant;
   h->tune.band = band;
   h->tune.threads = threads;

@@ -74,6 +74,7 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_W5H 12
 #define RT_VARIANT_W6 13
 #define RT_VARIANT_W2Z 14
+#define RT_VARIANT_SPLIT 15   // binary64: every face flux once, two passes (rt_split.cu)
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule
@@ -137,6 +138,14 @@ cudaError_t launch_batch_w6(const void* members, const long long* first, int nme
 // rt_persist.cu, rt_persist_w2.cu, rt_persist_ws.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);
+// two-pass binary64 step (rt_split.cu): the face fluxes of every axis with
+// n > 1 into f[a] (cell shape, the cell's right face) and f0[a] (face-0
+// plane, the layout of vlo[a]), then divergence, mean-flow term and update
+struct SplitFluxes {
+  double* f[6];
+  double* f0[6];
+};
+cudaError_t launch_step_split(const StepArgs<double>& A, const SplitFluxes& F, cudaStream_t st);
 // failure-detection self-test of the bounded waits (rt_persist.cu): one CTA
 // whose waits cannot complete; raises *status, leaves *completed at 0
 cudaError_t launch_wait_probe(int* status, int* completed, cudaStream_t st);

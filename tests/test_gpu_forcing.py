@@ -40,7 +40,7 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", list(CASES))
-@pytest.mark.parametrize("variant", ["tma", "plane", "cell"])
+@pytest.mark.parametrize("variant", ["tma", "plane", "cell", "split"])
 def test_forced_steps_bit_identical(name, variant):
     exp = CASES[name]()
     m = configs.build_model(exp, "fp64")

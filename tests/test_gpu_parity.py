@@ -76,7 +76,7 @@ SCHEDULES = [("tma", 8, 1024, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plan
              ("w2d", 4, 128, 0), ("w2d", 8, 256, 1), ("w3", 8, 256, 0), ("w3", 3, 512, 1),
              ("w3", 4, 128, 0), ("w4", 8, 512, 0), ("w4", 3, 256, 1), ("w4", 4, 128, 0), ("w5", 8, 512, 0),
              ("w5", 3, 256, 1), ("w5h", 4, 512, 0), ("w5h", 8, 256, 1), ("w6", 8, 256, 0), ("w6", 3, 512, 1),
-             ("w2z", 8, 512, 1), ("w2z", 3, 256, 0), ("cell", 8, 256, 0)]
+             ("w2z", 8, 512, 1), ("w2z", 3, 256, 0), ("cell", 8, 256, 0), ("split", 8, 256, 0)]
 
 
 @pytest.mark.parametrize("name", list(CASES))
