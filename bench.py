@@ -43,15 +43,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_key):
-    """per-cell DRAM bytes of a kernel from the committed ncu summary"""
+def profile_traffic(kernel_key, with_source=False):
+    """per-cell DRAM bytes of a kernel from the committed ncu summary (and
+    the summary it comes from)"""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if not os.path.exists(p):
-        return None
-    with open(p) as f:
-        d = json.load(f)
-    e = d.get(kernel_key)
-    return None if e is None else float(e["bytes_per_cell"])
+    e = None
+    if os.path.exists(p):
+        with open(p) as f:
+            e = json.load(f).get(kernel_key)
+    b = None if e is None else float(e["bytes_per_cell"])
+    return (b, None if e is None else e.get("source")) if with_source else b
 
 
 class ClockSampler:
@@ -312,11 +313,11 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
 def roofline(precision, cells, seconds_per_launch, traffic_key=None):
     peak, src = peaks()
     achieved = B_ALG[precision] * cells / seconds_per_launch / 1e9
-    tb = profile_traffic(traffic_key or "step_%s" % precision)
+    tb, tsrc = profile_traffic(traffic_key or "step_%s" % precision, with_source=True)
     return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src
             if src == "measured" else "fallback 6.8 TB/s",
-            "traffic": None if tb is None else tb * cells,
+            "traffic": None if tb is None else tb * cells, "traffic_source": tsrc,
             "alg_bytes_per_cell": B_ALG[precision]}
 
 
