@@ -4,7 +4,7 @@ import hashlib
 import numpy as np
 import pytest
 
-from golden_cases import NAMES, load
+from golden_cases import GPU_NAMES, NAMES, load
 from harness import build_oracle, configs, interior
 
 DIAG3 = ("E_int", "meanfl_int", "diss_ks", "diss_ke", "diss_ls", "diss_le", "diss_ms", "diss_me")
@@ -33,7 +33,7 @@ def test_oracle_reproduces_golden(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", GPU_NAMES)
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_gpu_against_golden(name, precision):
     import __graft_entry__ as g
