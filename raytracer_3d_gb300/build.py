@@ -2,7 +2,8 @@
 
 Each .cu translation unit is compiled by nvcc in parallel with
 -gencode arch=compute_103a,code=sm_103a, then linked into one shared
-library next to this file.  The binary64 parity arithmetic uses explicit
+library next to this file; the C++ host driver (host/rt_main.cpp) is then
+compiled with g++ against it.  The binary64 parity arithmetic uses explicit
 round-to-nearest intrinsics, so no global -fmad switch is needed.
 """
 import concurrent.futures as cf
@@ -38,7 +39,34 @@ def _deps():
     return max(os.path.getmtime(f) for f in files)
 
 
+HOST_SRC = os.path.join(HERE, "host", "rt_main.cpp")
+HOST_BIN = os.path.join(HERE, "host", "rt_main")
+
+
+def build_host(force=False):
+    """The C++ driver over the C ABI (host/rt_main.cpp, g++), linked
+    against the library next to it.  No fused multiply-add: its host grid
+    must equal the reference's bit for bit."""
+    deps = max(os.path.getmtime(f) for f in (HOST_SRC, LIB, os.path.join(INC, "rt_gb300.h")))
+    if not force and os.path.exists(HOST_BIN) and os.path.getmtime(HOST_BIN) >= deps:
+        return HOST_BIN
+    tmp = HOST_BIN + ".tmp"
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-Wall", HOST_SRC, "-I" + INC, "-L" + HERE,
+           "-lraytracer_gb300", "-Wl,-rpath," + HERE, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for the host driver:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, HOST_BIN)
+    return HOST_BIN
+
+
 def build(force=False, verbose=False):
+    lib = build_library(force, verbose)
+    build_host(force)
+    return lib
+
+
+def build_library(force=False, verbose=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
