@@ -1,0 +1,36 @@
+"""The bench's JSON contract on the CPU: the reference arm (the oracle port
+on the host cores) prints one line with the contract's keys, and the
+roofline helper reports the traffic figure with its source."""
+import json
+import os
+import subprocess
+import sys
+
+from harness import ROOT
+
+
+def test_reference_arm_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["warmup"] >= 3 and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["unit"] == line["unit"]
+    assert "workload" in line["config"]
+
+
+def test_roofline_reports_traffic_and_source():
+    sys.path.insert(0, ROOT)
+    import bench
+    cells = 32 ** 6
+    for key in ("step_fp64", "step_fp64_split", "step_fp32"):
+        prec = "fp32" if key.endswith("fp32") else "fp64"
+        rf = bench.roofline(prec, cells, 0.5, key)
+        assert rf["bound"] == "hbm" and rf["unit"] == "GB/s" and rf["traffic"] > 0
+        assert rf["traffic_source"].startswith("profiles/")
+        assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
+    assert [c[0] for c in bench.FP64_CANDIDATES] == ["tma", "split"]
