@@ -224,10 +224,13 @@ const char* rt_version(void);
  * Inactive axes (n = 1) may pass NULL.  Runs asynchronously on `stream`
  * (a cudaStream_t; NULL = legacy default stream).  Its scratch is a fixed
  * 256 KiB device array inside the library, so fields above 2^31 cells are
- * rejected with RT_ERR_ARG.  The first call on a device looks up that
- * array's address and must come before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race.  Errors are described by
- * rt_noalloc_last_error(). */
+ * rejected with RT_ERR_ARG (as is onx != 2).  The first call on a device
+ * looks up that array's address and must come before any stream capture;
+ * the address is kept for the device's primary context, so after a
+ * cudaDeviceReset the entry point must not be called on that device again.
+ * All calls share the array: calls that overlap on the GPU race.  Errors
+ * are described by rt_noalloc_last_error(), which returns the calling
+ * thread's own last message. */
 int rt_max_rate_noalloc(const rt_dims* dims, const double* const* vel, const double* const* vlo,
                         const double* const* dgrid, double* out, void* stream);
 const char* rt_noalloc_last_error(void);

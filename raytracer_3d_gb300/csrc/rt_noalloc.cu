@@ -96,11 +96,16 @@ __global__ void __launch_bounds__(RT_NOALLOC_THREADS)
 
 using namespace rt;
 
-// device address of the scratch array, looked up once per device
+// device address of the scratch array, looked up once per device.  The
+// address belongs to the device's primary context: after cudaDeviceReset
+// the cached value is stale, so a process that resets a device must not
+// call rt_max_rate_noalloc on it again.
 #define RT_NOALLOC_MAX_DEVICES 64
 static double* g_scratch_ptr[RT_NOALLOC_MAX_DEVICES];
 static std::mutex g_scratch_mu;
-static std::string g_noalloc_err;
+// message of the calling thread's last failed call (one buffer per thread,
+// so concurrent callers neither race on it nor see each other's text)
+static thread_local std::string g_noalloc_err;
 
 static int noalloc_fail(int code, const std::string& msg) {
   g_noalloc_err = msg;
@@ -115,22 +120,24 @@ int rt_max_rate_noalloc(const rt_dims* dims, const double* const* vel, const dou
                         const double* const* dgrid, double* out, void* stream) {
   if (!dims || !vel || !vlo || !dgrid || !out)
     return noalloc_fail(RT_ERR_ARG, "rt_max_rate_noalloc: NULL argument");
+  // the grid spacings are indexed with the library's halo width
+  if (dims->onx != RT_ONX)
+    return noalloc_fail(RT_ERR_ARG, "rt_max_rate_noalloc: onx must be " + std::to_string(RT_ONX));
   const int nn[6] = {dims->nx, dims->ny, dims->nz, dims->nk, dims->nl, dims->nm};
   Dims d{};
   long long st = 1;
   for (int a = 0; a < 6; a++) {
     if (nn[a] < 1) return noalloc_fail(RT_ERR_ARG, "rt_max_rate_noalloc: an axis has no points");
+    // checked before multiplying, so the running product cannot overflow
+    if (st > RT_NOALLOC_MAX_CELLS / nn[a])
+      return noalloc_fail(RT_ERR_ARG, "rt_max_rate_noalloc: the field's cells exceed the limit of its fixed "
+                                      "scratch (" + std::to_string(RT_NOALLOC_MAX_CELLS) + " cells)");
     d.n[a] = nn[a];
     d.s[a] = st;
     st *= nn[a];
   }
   d.ncell = st;
   fill_plane_strides(d);
-  if (d.ncell > RT_NOALLOC_MAX_CELLS)
-    return noalloc_fail(RT_ERR_ARG,
-                        "rt_max_rate_noalloc: " + std::to_string(d.ncell) +
-                            " cells exceed the limit of its fixed scratch (" +
-                            std::to_string(RT_NOALLOC_MAX_CELLS) + " cells)");
   ConstVel v{};
   for (int a = 0; a < 6; a++) {
     if (nn[a] > 1 && (!vel[a] || !vlo[a] || !dgrid[a]))

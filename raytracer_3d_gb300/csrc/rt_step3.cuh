@@ -57,7 +57,13 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 
 // bounded wait; returns false (and raises the status flag) on timeout.
-// LIMIT polls (the failure-detection self-test uses a short one)
+// LIMIT polls (the failure-detection self-test uses a short one).  After a
+// timeout the caller's copies get a second LIMIT polls to land; a copy that
+// has not landed by then is abandoned when the CTA leaves (its shared memory
+// may be handed to another CTA), so the flagged launch's results, and those
+// of any launch that overlaps it, are invalid -- which is what the raised
+// status tells the host.  No CTA issues a copy after one of its own waits
+// has timed out.
 template <uint32_t LIMIT = RT_WAIT_LIMIT>
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
   for (uint32_t it = 0; it < LIMIT; it++)

@@ -74,3 +74,20 @@ def test_timers_and_selftest_reject_null_arguments(lib):
     assert lib.rt_timing_secs(None, b"integrate", ctypes.byref(secs), None) == -1
     assert lib.rt_selftest_wait_timeout(None, None) == -1
     assert lib.rt_get_tendency(None, None, None) == -1
+
+
+def test_noalloc_rejects_bad_dims_without_gpu(lib):
+    """the allocation-free rate rejects a halo width other than 2 and a
+    cell count beyond its fixed scratch, including products that would
+    overflow a 64-bit integer (six axes of 65536 = 2^96 cells), before any
+    CUDA call"""
+    from raytracer_3d_gb300 import _lib
+    P = ctypes.POINTER(ctypes.c_double)
+    null6 = (P * 6)()
+    out = ctypes.cast(1, P)
+    for dims, word in ((_lib.RtDims(8, 8, 8, 8, 8, 8, 3), b"onx"),
+                       (_lib.RtDims(*([65536] * 6), 2), b"exceed"),
+                       (_lib.RtDims(2, 2, 2, 2, 2, 2 ** 30, 2), b"exceed")):
+        rc = lib.rt_max_rate_noalloc(ctypes.byref(dims), null6, null6, null6, out, None)
+        assert rc == -1
+        assert word in lib.rt_noalloc_last_error()
