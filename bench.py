@@ -184,9 +184,54 @@ FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w2d", "w6") for t in (1
                       for s in (0, 1)])
 
 
-# binary64: the fused plane kernel, or the two-pass step that evaluates every
-# face flux once (FP64-pipe bound either way); dry steps pick the faster
-FP64_CANDIDATES = [("tma", 8, 256, 0), ("split", 8, 256, 0)]
+# binary64: the fused plane kernel, the two-pass step that evaluates every
+# face flux once (both bit-identical to the reference's arithmetic), or the
+# two-pass step without divisions (within 1e-12 relative per step); all are
+# bound by the binary64 pipe, and dry steps pick the fastest
+FP64_CANDIDATES = [("tma", 8, 256, 0), ("split", 8, 256, 0), ("fast", 8, 256, 0)]
+
+
+def fp64_ops_per_cell(schedule, n):
+    """binary64 pipe instructions (add, multiply, fma; each counted once) per
+    cell-update of the fast schedule, from its source: per axis with n > 1,
+    4 per face flux (Rj, the upwind difference, v*E_up, the fma with h) on
+    n + 1 faces per n cells, and 2 in the update (F_l - F_r, the fma with
+    dt/d); plus the final fma with mu.  None for the bit-exact schedules,
+    whose divisions and comparisons are compiler sequences (their counts
+    come from ncu, profiles/)."""
+    if schedule != "fast":
+        return None
+    ops = 1.0
+    for k in n:
+        if k > 1:
+            ops += 4.0 * (1.0 + 1.0 / k) + 2.0
+    return ops
+
+
+def fp64_peak():
+    """binary64 fma instructions per second of this GPU (rt_fp64_rate, best
+    of three), with the clocks seen while it ran"""
+    import ctypes
+    import torch
+    from raytracer_3d_gb300 import _lib
+    lib = _lib.load()
+    best = 0.0
+    with ClockSampler(torch.cuda.current_device()) as cs:
+        for _ in range(3):
+            r = ctypes.c_double()
+            if lib.rt_fp64_rate(ctypes.byref(r)) == 0:
+                best = max(best, r.value)
+    return {"fma_per_s": best, "clocks": cs.summary(),
+            "how": "rt_fp64_rate: 8 independent fma chains per thread, 8 CTAs of 256 threads per SM, "
+                   "2^14 iterations, CUDA events, best of 3"}
+
+
+SCHEDULE_NOTES = {
+    "fast": "two passes without divisions (rt_fast.cu): within 1e-12 relative L-inf of the reference per step, "
+            "not bit-identical",
+    "split": "two passes, the reference's arithmetic bit for bit (rt_split.cu)",
+    "tma": "fused plane kernel, the reference's arithmetic bit for bit (rt_step3.cuh)",
+}
 
 
 def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False, candidates=None):
@@ -310,15 +355,28 @@ def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
                                    "p50_s": sb["p50_s"], "p99_s": sb["p99_s"]}}
 
 
-def roofline(precision, cells, seconds_per_launch, traffic_key=None):
+def roofline(precision, cells, seconds_per_launch, traffic_key=None, fp64=None):
+    """HBM roofline of one step (algorithmic bytes per cell x cells / step
+    time against the measured copy bandwidth); for the binary64 form, given
+    fp64 = (ops per cell, measured fma/s), the binary64-pipe roofline that
+    bounds it, with the HBM figures beside it"""
     peak, src = peaks()
     achieved = B_ALG[precision] * cells / seconds_per_launch / 1e9
     tb, tsrc = profile_traffic(traffic_key or "step_%s" % precision, with_source=True)
-    return {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src
-            if src == "measured" else "fallback 6.8 TB/s",
-            "traffic": None if tb is None else tb * cells, "traffic_source": tsrc,
-            "alg_bytes_per_cell": B_ALG[precision]}
+    hbm = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+           "frac": round(achieved / peak, 4), "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % src
+           if src == "measured" else "fallback 6.8 TB/s",
+           "traffic": None if tb is None else tb * cells, "traffic_source": tsrc,
+           "alg_bytes_per_cell": B_ALG[precision]}
+    if fp64 is None or fp64[0] is None or not fp64[1]:
+        return hbm
+    ops, rate = fp64
+    got = ops * cells / seconds_per_launch / 1e9
+    return {"bound": "fp64", "achieved": round(got, 2), "peak": round(rate / 1e9, 2),
+            "unit": "G binary64 ops/s", "frac": round(got / (rate / 1e9), 4),
+            "peak_source": "measured in this run (rt_fp64_rate: binary64 fma instructions/s)",
+            "ops_per_cell": round(ops, 4), "traffic": hbm["traffic"], "traffic_source": tsrc,
+            "hbm": {k: hbm[k] for k in ("achieved", "peak", "unit", "frac", "peak_source", "alg_bytes_per_cell")}}
 
 
 def gpu_arm(args):
@@ -348,10 +406,14 @@ def gpu_arm(args):
         return
     # the binary64 form is bound by the FP64 pipe; 256-thread CTAs keep its
     # registers unspilled (the flags set the fp32 schedule when --tune 0)
-    main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, FP64_CANDIDATES[0],
-                    tune=args.tune, candidates=FP64_CANDIDATES)
+    peak64 = fp64_peak()
+    if args.fp64_variant:
+        main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, (args.fp64_variant, 8, 256, 0))
+    else:
+        main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, FP64_CANDIDATES[-1],
+                        tune=args.tune, candidates=FP64_CANDIDATES)
     f64_sched = tuple(main["schedule"])
-    f64_split = f64_sched[0] == "split"
+    f64_key = {"split": "step_fp64_split", "fast": "step_fp64_fast"}.get(f64_sched[0], "step_fp64")
     forms = {}
     if not args.no_fp32:
         f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
@@ -374,10 +436,12 @@ def gpu_arm(args):
         "data": "synthetic (seeded log-normal spectrum, analytic N(z), U(y,z))",
         "config": {"workload": "jet_large %d^3x%d^3 plain fp64, CFL 0.4 (dt=%%.6g s)" % (n[0], n[0]) % main["dt"],
                    "cells": cells, "form": "fp64", "schedule": "%s band %d threads %d sweep %d" % f64_sched,
+                   "schedule_note": SCHEDULE_NOTES.get(f64_sched[0], ""),
                    "tuning_table_ms": main["tuning_table_ms"], "l2": "state 8.6 GB per field >> L2; no flush needed",
                    "parallelism": "replicas x%d" % world},
-        "roofline": roofline("fp64", cells, main["seconds"] / args.steps,
-                             "step_fp64_split" if f64_split else "step_fp64"),
+        "roofline": roofline("fp64", cells, main["seconds"] / args.steps, f64_key,
+                             fp64=(fp64_ops_per_cell(f64_sched[0], n), peak64["fma_per_s"])),
+        "fp64_peak": peak64,
         "clocks": main["clocks"],
         "gpu_launches": main["launches"],
     }
@@ -429,6 +493,8 @@ def main():
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
     ap.add_argument("--dims", default=None, help="nx,ny,nz,nk,nl,nm of a profiling case (with --no-fp64)")
     ap.add_argument("--variant", default="tma", choices=("w2z", "w6", "w5", "w5h", "w4", "w3", "w2", "w2d", "ws", "wsd", "pipe", "tma", "group", "plane", "cell"))
+    ap.add_argument("--fp64-variant", default=None, choices=("tma", "split", "fast"),
+                    help="binary64 schedule (default: the fastest of the candidates by dry steps)")
     ap.add_argument("--band", type=int, default=8)
     ap.add_argument("--threads", type=int, default=1024)
     ap.add_argument("--sweep", type=int, default=0)

@@ -287,6 +287,12 @@ int rt_tic(rt_handle* h, const char* name);
 int rt_toc(rt_handle* h, const char* name);
 int rt_timing_secs(rt_handle* h, const char* name, double* secs, long long* calls);
 
+/* Binary64 fused multiply-add instructions per second of the current GPU,
+ * measured by a short kernel of independent fma chains timed with CUDA
+ * events.  No counterpart in the reference: the denominator of the
+ * roofline of the binary64 step, which GB300's binary64 pipe bounds. */
+int rt_fp64_rate(double* fma_per_s);
+
 /* Failure-detection self-test of the bounded device waits.  Every wait of
  * the step kernels on an mbarrier gives up after a fixed number of polls,
  * raises a status flag that the next synchronising call turns into

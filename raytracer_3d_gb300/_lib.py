@@ -64,6 +64,7 @@ SIGNATURES = {
     "rt_toc": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "rt_timing_secs": (ctypes.c_int, [_P, ctypes.c_char_p, _D, ctypes.POINTER(ctypes.c_longlong)]),
     "rt_selftest_wait_timeout": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "rt_fp64_rate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "rt_set_host_access": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_set_state_interior": (ctypes.c_int, [_P, _P]),
     "rt_get_state_interior": (ctypes.c_int, [_P, _P]),

@@ -52,6 +52,9 @@ struct rt_handle {
   long long force_gen = 0;      // changes with every rt_set_forcing
   double dzt1 = 0.0;            // dzt(1), the bottom cell's spacing
   SplitFluxes split{};          // flux fields of the two-pass binary64 step (allocated on selection)
+  double* mu = nullptr;         // fast binary64 step: 1 - dt*lambda per cell (allocated on selection)
+  double* tab64 = nullptr;      // and its tables dt/d_a (offsets toff[0..5])
+  int uc_holds = 0;             // uc/ucl hold 0: uCFL of the bit-exact kernels, 1: h of the fast step
   double* scratch = nullptr;    // reductions
   long long scratch_len = 0;
   double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
@@ -227,9 +230,48 @@ static cudaError_t apply_forcing(rt_handle* h, int buf, cudaStream_t st) {
                                h->forcing, st);
 }
 
+// the per-face values in uc/ucl for the kind of binary64 step about to run:
+// uCFL for the bit-exact kernels (kind 0), h, mu and the tables for the fast
+// step (kind 1); recomputed only when the kind changes (or dt / the
+// coefficients did, which resets uc_holds)
+static cudaError_t ensure_uc(rt_handle* h, int kind) {
+  if (h->uc_holds == kind) return cudaSuccess;
+  const double* vel[6];
+  const double* vlo[6];
+  for (int a = 0; a < 6; a++) { vel[a] = (const double*)h->vel[a]; vlo[a] = (const double*)h->vlo[a]; }
+  cudaError_t e;
+  if (kind == 0) {
+    e = launch_ucfl(h->d, make_grid(h), h->p.dt, vel, vlo, h->uc, h->ucl, h->st);
+    h->launches += 6;
+  } else {
+    const double* lam[3] = {(const double*)h->lam[0], (const double*)h->lam[1], (const double*)h->lam[2]};
+    e = launch_fast_prepare(h->d, make_grid(h), h->p.dt, vel, vlo, lam, h->uc, h->ucl, h->mu, h->tab64, h->toff,
+                            h->st);
+    h->launches += 7;
+  }
+  if (e == cudaSuccess) h->uc_holds = kind;
+  return e;
+}
+
+static bool fast_ready(const rt_handle* h) {
+  bool split = false;
+  for (int a = 0; a < 6; a++) split = split || h->split.f[a] != nullptr;
+  return split && h->mu && h->tab64;
+}
+
 // one step of the handle from buffer src into 1 - src; returns the kernels launched
 static cudaError_t step_once(rt_handle* h, int src, int* nlaunch) {
   if (h->p.precision == RT_FP64) {
+    if (h->tune.variant == RT_VARIANT_FAST && fast_ready(h)) {
+      cudaError_t e = ensure_uc(h, 1);
+      if (e != cudaSuccess) return e;
+      FastTab T;
+      for (int a = 0; a < 6; a++) T.c[a] = h->tab64 + h->toff[a];
+      *nlaunch = 2;
+      return launch_step_fast(make_step_args<double>(h, src), h->split, h->mu, T, h->st);
+    }
+    cudaError_t e = ensure_uc(h, 0);
+    if (e != cudaSuccess) return e;
     // the two-pass step once its fields exist (rt_set_tuning allocates them;
     // a field with no axis longer than one keeps the fused step)
     bool split = false;
@@ -257,14 +299,21 @@ static int ensure_split(rt_handle* h) {
   return RT_OK;
 }
 
-// binary64 form: refresh the cached uCFL fields (after the coefficients or dt change)
+// fast binary64 step: mu and the tables (its flux fields are the two-pass step's)
+static int ensure_fast(rt_handle* h) {
+  int rc = ensure_split(h);
+  if (!rc && !h->mu) rc = dev_alloc(h, (void**)&h->mu, (size_t)h->d.ncell * sizeof(double));
+  if (!rc && !h->tab64) rc = dev_alloc(h, (void**)&h->tab64, (size_t)h->toff[6] * sizeof(double));
+  return rc;
+}
+
+// binary64 form: refresh the cached per-face values (after the coefficients
+// or dt change) for the kind of step selected
 static int refresh_ucfl(rt_handle* h) {
   if (h->p.precision != RT_FP64 || !h->have_coeff) return RT_OK;
-  const double* vel[6];
-  const double* vlo[6];
-  for (int a = 0; a < 6; a++) { vel[a] = (const double*)h->vel[a]; vlo[a] = (const double*)h->vlo[a]; }
-  cudaError_t e = launch_ucfl(h->d, make_grid(h), h->p.dt, vel, vlo, h->uc, h->ucl, h->st);
-  h->launches += 6;
+  h->uc_holds = -1;
+  const int kind = h->tune.variant == RT_VARIANT_FAST && fast_ready(h) ? 1 : 0;
+  cudaError_t e = ensure_uc(h, kind);
   if (e != cudaSuccess) return fail(h, RT_ERR_CUDA, "uCFL: %s", cudaGetErrorString(e));
   return RT_OK;
 }
@@ -602,6 +651,13 @@ static int batch_run(rt_batch* b, int nsteps) {
     if (b->mem[j]->cur != (b->cur0[j] ^ b->parity) || b->fgen.size() != (size_t)n ||
         b->mem[j]->force_gen != b->fgen[j])
       b->dirty = true;
+  // binary64 members: the batch kernels read uCFL, which a member's own fast
+  // steps may have replaced (queued on the member's stream, ordered below)
+  for (int j = 0; j < n; j++)
+    if (b->mem[j]->p.precision == RT_FP64 && b->mem[j]->uc_holds != 0) {
+      cudaError_t e = ensure_uc(b->mem[j], 0);
+      if (e != cudaSuccess) return bfail(b, RT_ERR_CUDA, "uCFL: %s", cudaGetErrorString(e));
+    }
   // the batch stream runs after everything queued on the members' streams
   for (int j = 0; j < n; j++) {
     BCUDA_TRY(b, cudaEventRecord(b->mem[j]->ev, b->mem[j]->st));
@@ -915,6 +971,8 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->status);
   cudaFree(h->force);
   for (int a = 0; a < 6; a++) { cudaFree(h->split.f[a]); cudaFree(h->split.f0[a]); }
+  cudaFree(h->mu);
+  cudaFree(h->tab64);
   for (auto& kv : h->timers) {
     if (kv.second.open) cudaEventDestroy(kv.second.open);
     for (auto& pr : kv.second.pairs) {
@@ -1450,13 +1508,17 @@ int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
       variant != RT_VARIANT_WSD && variant != RT_VARIANT_W2 && variant != RT_VARIANT_W2D &&
       variant != RT_VARIANT_W3 && variant != RT_VARIANT_W4 && variant != RT_VARIANT_W5 &&
       variant != RT_VARIANT_W5H && variant != RT_VARIANT_W6 && variant != RT_VARIANT_W2Z &&
-      variant != RT_VARIANT_SPLIT)
+      variant != RT_VARIANT_SPLIT && variant != RT_VARIANT_FAST)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
   if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: threads must be 128, 256, 512 or 1024");
   if (variant == RT_VARIANT_SPLIT && h->p.precision == RT_FP64) {
     const int rc = ensure_split(h);
+    if (rc) return rc;
+  }
+  if (variant == RT_VARIANT_FAST && h->p.precision == RT_FP64) {
+    const int rc = ensure_fast(h);
     if (rc) return rc;
   }
   h->tune.variant = variant;

@@ -75,6 +75,7 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_W6 13
 #define RT_VARIANT_W2Z 14
 #define RT_VARIANT_SPLIT 15   // binary64: every face flux once, two passes (rt_split.cu)
+#define RT_VARIANT_FAST 16    // binary64: two passes without divisions (rt_fast.cu), within 1e-12 of the reference
 struct StepTuning {
   int variant = RT_VARIANT_TMA;
   int band = 8;       // values per band of the plane schedule
@@ -146,6 +147,19 @@ struct SplitFluxes {
   double* f0[6];
 };
 cudaError_t launch_step_split(const StepArgs<double>& A, const SplitFluxes& F, cudaStream_t st);
+// fast binary64 step (rt_fast.cu): the flux fields of the two-pass step,
+// h = |v|/2*(1-|v dt/d|) per face (hr: right faces, hl: face-0 planes),
+// mu = 1 - dt*lambda per cell and the per-axis tables c[a] = dt/d_a on the
+// padded index range
+struct FastTab {
+  const double* c[6];
+};
+cudaError_t launch_fast_prepare(const Dims& d, const Grid& g, double dt, const double* const* vel,
+                                const double* const* vlo, const double* const* lam, double* const* hr,
+                                double* const* hl, double* mu, double* tab, const long long* toff,
+                                cudaStream_t st);
+cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, const double* mu, const FastTab& T,
+                             cudaStream_t st);
 // failure-detection self-test of the bounded waits (rt_persist.cu): one CTA
 // whose waits cannot complete; raises *status, leaves *completed at 0
 cudaError_t launch_wait_probe(int* status, int* completed, cudaStream_t st);

@@ -1,0 +1,74 @@
+// rt_probe.cu -- measured binary64 rate of the GPU, the denominator of the
+// roofline of the binary64 step (which is bound by the binary64 pipe, not
+// by HBM, on GB300).
+//
+// Every thread runs RT_PROBE_CHAINS independent fused multiply-add chains
+// x = fma(x, a, b) for `iters` iterations; the chains keep the pipe fed
+// without depending on one another.  The result is the number of binary64
+// fma instructions per second of the whole GPU, timed with CUDA events on a
+// second launch (the first warms the clocks and the instruction cache).
+#include <cuda_runtime.h>
+
+#include "../../include/rt_gb300.h"
+
+namespace rt {
+
+#define RT_PROBE_CHAINS 8
+#define RT_PROBE_THREADS 256
+
+__global__ void __launch_bounds__(RT_PROBE_THREADS) fp64_fma_probe(int iters, double a, double b, double* sink) {
+  double x[RT_PROBE_CHAINS];
+#pragma unroll
+  for (int c = 0; c < RT_PROBE_CHAINS; c++) x[c] = (double)(threadIdx.x + c) * 1e-3;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < RT_PROBE_CHAINS; c++) x[c] = __fma_rn(x[c], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < RT_PROBE_CHAINS; c++) s += x[c];
+  if (s == 12345.678) sink[0] = s;   // never true for the chosen a, b: keeps the chains live
+}
+
+}  // namespace rt
+
+extern "C" int rt_fp64_rate(double* fma_per_s) {
+  using namespace rt;
+  if (!fma_per_s) return RT_ERR_ARG;
+  *fma_per_s = 0.0;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return RT_ERR_CUDA;
+  }
+  double* sink = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = RT_OK;
+  const int blocks = nsm * 8;
+  const int iters = 1 << 14;
+  float ms = 0.f;
+  if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) ||
+      cudaEventCreate(&e0) || cudaEventCreate(&e1)) {
+    rc = RT_ERR_CUDA;
+    goto done;
+  }
+  // a slightly below 1 and b small keep x bounded and normal
+  fp64_fma_probe<<<blocks, RT_PROBE_THREADS, 0, st>>>(iters, 0.999999, 1e-6, sink);
+  cudaEventRecord(e0, st);
+  fp64_fma_probe<<<blocks, RT_PROBE_THREADS, 0, st>>>(iters, 0.999999, 1e-6, sink);
+  cudaEventRecord(e1, st);
+  if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f) {
+    rc = RT_ERR_CUDA;
+    goto done;
+  }
+  *fma_per_s = (double)blocks * RT_PROBE_THREADS * RT_PROBE_CHAINS * (double)iters / (ms * 1e-3);
+done:
+  cudaGetLastError();
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (sink) cudaFree(sink);
+  return rc;
+}

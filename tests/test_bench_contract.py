@@ -33,4 +33,23 @@ def test_roofline_reports_traffic_and_source():
         assert rf["bound"] == "hbm" and rf["unit"] == "GB/s" and rf["traffic"] > 0
         assert rf["traffic_source"].startswith("profiles/")
         assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
-    assert [c[0] for c in bench.FP64_CANDIDATES] == ["tma", "split"]
+    assert [c[0] for c in bench.FP64_CANDIDATES] == ["tma", "split", "fast"]
+
+
+def test_fp64_roofline_is_bound_by_the_fp64_pipe():
+    """the binary64 line reports the binary64-pipe roofline (ops per cell of
+    the fast schedule from its source, measured fma rate) with the HBM
+    fraction beside it"""
+    sys.path.insert(0, ROOT)
+    import bench
+    n = (32,) * 6
+    ops = bench.fp64_ops_per_cell("fast", n)
+    assert abs(ops - (1 + 6 * (4 * (1 + 1 / 32) + 2))) < 1e-12
+    assert bench.fp64_ops_per_cell("split", n) is None
+    assert bench.fp64_ops_per_cell("fast", (8, 1, 1, 1, 1, 8)) == 1 + 2 * (4 * (1 + 1 / 8) + 2)
+    rf = bench.roofline("fp64", 32 ** 6, 0.1, "step_fp64_split", fp64=(ops, 5e11))
+    assert rf["bound"] == "fp64" and rf["unit"] == "G binary64 ops/s"
+    assert abs(rf["achieved"] - ops * 32 ** 6 / 0.1 / 1e9) < 0.01
+    assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
+    assert rf["hbm"]["unit"] == "GB/s" and rf["hbm"]["alg_bytes_per_cell"] == 72
+    assert bench.roofline("fp64", 32 ** 6, 0.1, "step_fp64_split", fp64=(None, 5e11))["bound"] == "hbm"

@@ -98,6 +98,111 @@ def test_steps_bit_identical(name, sched):
         m.close()
 
 
+@pytest.mark.parametrize("name", list(CASES))
+def test_fast_fp64_within_bound(name):
+    """the fast binary64 schedule (no divisions, integer-selected limiter,
+    regrouped update) stays within the plain form's bound of 1e-12 relative
+    L-infinity of the oracle at every step"""
+    exp, m, o = _pair(name)
+    m.set_tuning("fast", 8, 256)
+    sl = interior(exp.n)
+    worst = 0.0
+    try:
+        for s in range(4):
+            m.integrate(1)
+            o.integrate(1)
+            m.get_state()
+            rel = max_rel(m.E[sl], o.E[sl])
+            worst = max(worst, rel)
+            assert rel <= FP64_STEP_TOL, (s, rel)
+        print("%s: fast binary64 within %.2e of the oracle over 4 steps" % (name, worst))
+    finally:
+        m.close()
+
+
+def test_fast_fp64_switches_with_bit_exact_schedules():
+    """switching between the fast and the bit-exact schedules on one handle
+    (the per-face cache changes meaning between uCFL and h) keeps every
+    step on its own bound: each step starts from the oracle's state"""
+    exp, m, o = _pair("shear_mini")
+    sl = interior(exp.n)
+    try:
+        for sched in ("fast", "tma", "fast", "split", "plane", "fast", "group"):
+            m.E[sl] = o.E[sl]
+            m.set_state()
+            m.set_tuning(sched, 8, 256)
+            m.integrate(1)
+            o.integrate(1)
+            m.get_state()
+            if sched == "fast":
+                assert max_rel(m.E[sl], o.E[sl]) <= FP64_STEP_TOL, sched
+            else:
+                assert np.array_equal(m.E[sl], o.E[sl]), sched
+    finally:
+        m.close()
+
+
+def _vol(o, n):
+    vol = np.ones(n)
+    for a in range(6):
+        shp = [1] * 6
+        shp[a] = n[a]
+        vol = vol * o.grid["xyzklm"[a]]["dt"][ONX:ONX + n[a]].reshape(shp)
+    return vol
+
+
+def test_config1_packet_200_steps():
+    """the 8x8x16 x 16^3 packet workload run to its full 200 steps: the
+    two-pass bit-exact schedule equals the oracle bit for bit at every
+    snapshot step, the fast schedule stays within 1e-12 relative L-infinity,
+    and after the last step the budget (diagnose.f90:46-329) matches the
+    oracle's, with a residual at round-off and the total energy sum(E*vol)
+    equal"""
+    exp = CASES["packet_small"]()
+    o = build_oracle(exp, threads=True)
+    exact = configs.build_model(exp, "fp64")
+    fast = configs.build_model(exp, "fp64")
+    exact.set_tuning("split", 8, 256)
+    fast.set_tuning("fast", 8, 256)
+    sl = interior(exp.n)
+    vol = _vol(o, exp.n)
+    checks = (1, 2, 5, 10, 20, 50, 100, 150, 200)
+    done = 0
+    worst = 0.0
+    try:
+        for step in checks:
+            k = step - done
+            exact.integrate(k)
+            fast.integrate(k)
+            o.integrate(k)
+            done = step
+            ref = o.E[sl]
+            got = exact.get_state()[sl]
+            assert np.array_equal(got, ref), (step, max_rel(got, ref))
+            rel = max_rel(fast.get_state()[sl], ref)
+            worst = max(worst, rel)
+            assert rel <= FP64_STEP_TOL, (step, rel)
+        b, _ = exact.diagnose(fields=False)
+        bf, _ = fast.diagnose(fields=False)
+        bo = o.diagnose()
+        sums = [k for k in bo if k in ("eint", "mflint") or k.startswith("bfl")]
+        scale = sum(abs(bo[k]) for k in sums)
+        for k in sums:
+            assert abs(b[k] - bo[k]) <= 1e-12 * max(abs(bo[k]), 1e-300) + 1e-15 * scale, (k, b[k], bo[k])
+        assert abs(b["residual"]) <= 1e-12 * scale
+        assert abs(bf["residual"]) <= 1e-12 * scale
+        e_ref = float(np.sum(o.E[sl] * vol))
+        e_exact = float(np.sum(exact.E[sl] * vol))
+        e_fast = float(np.sum(fast.E[sl] * vol))
+        assert e_exact == e_ref
+        assert abs(e_fast - e_ref) <= 1e-12 * abs(e_ref)
+        print("config 1, 200 steps: split bit-identical at %s; fast within %.2e (L-inf), energy %.3e (rel); "
+              "residual %.2e of %.2e" % (checks, worst, abs(e_fast - e_ref) / abs(e_ref), b["residual"], scale))
+    finally:
+        exact.close()
+        fast.close()
+
+
 @pytest.mark.parametrize("name", ["shear_mini", "shear_open", "ragged", "section_2d", "column_1d"])
 def test_budget_matches_diagnose(name):
     exp, m, o = _pair(name)

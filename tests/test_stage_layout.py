@@ -34,3 +34,19 @@ def test_stage_copy_lists_match_barrier_bytes():
         print(r.stdout)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "0 failures" in r.stdout
+
+
+def test_fast_superbee_selection_is_exact():
+    """the fast binary64 step's division-free limiter (integer selection of
+    Rj, up or twice one of them) equals phi(up/Rj)*Rj exactly and the
+    reference's division form to rounding, over special and random cases"""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "superbee_select_check")
+        cmd = [_nvcc(), "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC,
+               os.path.join(HERE, "native", "superbee_select_check.cu"), "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+        print(r.stdout)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert " 0 failures" in r.stdout
