@@ -177,11 +177,9 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w2d", "w6") for t in (128, 256, 512) for b in (4, 8)
+FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w3", "w6") for t in (128, 256, 512) for b in (4, 8)
                     for s in (0, 1)]
-                   + [("w2", b, t, s) for t in (256, 512) for b in (4, 8) for s in (0, 1)]
-                   + [(v, b, t, s) for v in ("pipe", "tma") for t in (256, 512, 1024) for b in (4, 8)
-                      for s in (0, 1)])
+                   + [("tma", b, t, s) for t in (256, 512, 1024) for b in (4, 8) for s in (0, 1)])
 
 
 # binary64: the fused plane kernel, the two-pass step that evaluates every
@@ -492,7 +490,7 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
     ap.add_argument("--dims", default=None, help="nx,ny,nz,nk,nl,nm of a profiling case (with --no-fp64)")
-    ap.add_argument("--variant", default="tma", choices=("w2z", "w6", "w5", "w5h", "w4", "w3", "w2", "w2d", "ws", "wsd", "pipe", "tma", "group", "plane", "cell"))
+    ap.add_argument("--variant", default="tma", choices=("w2z", "w6", "w3", "tma", "group", "plane", "cell"))
     ap.add_argument("--fp64-variant", default=None, choices=("tma", "split", "fast"),
                     help="binary64 schedule (default: the fastest of the candidates by dry steps)")
     ap.add_argument("--band", type=int, default=8)

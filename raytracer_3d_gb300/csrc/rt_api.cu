@@ -1504,11 +1504,8 @@ int rt_timing_secs(rt_handle* h, const char* name, double* secs, long long* call
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
   if (!h) return RT_ERR_ARG;
   if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA &&
-      variant != RT_VARIANT_GROUP && variant != RT_VARIANT_PIPE && variant != RT_VARIANT_WS &&
-      variant != RT_VARIANT_WSD && variant != RT_VARIANT_W2 && variant != RT_VARIANT_W2D &&
-      variant != RT_VARIANT_W3 && variant != RT_VARIANT_W4 && variant != RT_VARIANT_W5 &&
-      variant != RT_VARIANT_W5H && variant != RT_VARIANT_W6 && variant != RT_VARIANT_W2Z &&
-      variant != RT_VARIANT_SPLIT && variant != RT_VARIANT_FAST)
+      variant != RT_VARIANT_GROUP && variant != RT_VARIANT_W3 && variant != RT_VARIANT_W6 &&
+      variant != RT_VARIANT_W2Z && variant != RT_VARIANT_SPLIT && variant != RT_VARIANT_FAST)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);
   if (band < 1 || band > 1024) return fail(h, RT_ERR_ARG, "rt_set_tuning: band %d out of range", band);
   if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)

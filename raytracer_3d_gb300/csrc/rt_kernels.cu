@@ -684,7 +684,7 @@ cudaError_t launch_step(const StepArgs<T>& A, const StepTuning& tn, cudaStream_t
       return launch_group_nt<T, 256>(A, S, nblk, st);
     }
   }
-  if ((tn.variant == RT_VARIANT_TMA || tn.variant >= RT_VARIANT_PIPE) &&
+  if ((tn.variant == RT_VARIANT_TMA || tn.variant >= RT_VARIANT_W3) &&
       tma_path_ok<T>(A.d) &&
       tma_maxc((long long)A.d.n[0] * A.d.n[1], tn.threads) <= RT_TMA_MAXC) {
     const PlaneSched S = make_sched(A.d, tn);

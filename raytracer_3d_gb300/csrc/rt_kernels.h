@@ -56,24 +56,20 @@ cudaError_t launch_ucfl(const Dims& d, const Grid& g, double dt, const double* c
                         cudaStream_t st);
 cudaError_t launch_lam_combine(const double* lx, const double* ly, const double* lz, int ux, int uy,
                                int uz, float* dst, long long n, cudaStream_t st);
-// step kernel variants: the plane-tiled kernel (rt_step2.cuh) and the
-// one-thread-per-cell kernel (rt_step.cuh), kept as the fallback for planes
-// that do not fit in shared memory
+// step kernel variants (numbers are the rt_set_tuning codes): the
+// plane-tiled kernel (rt_step2.cuh), the one-thread-per-cell kernel
+// (rt_step.cuh), kept as the fallback for planes that do not fit in shared
+// memory, the TMA-staged plane and z-group kernels (rt_step3.cuh,
+// rt_step4.cuh) and the persistent binary32 kernels (rt_step7.cuh,
+// rt_step8.cuh, rt_step11.cuh).  Codes 4-8 and 10-12 belonged to earlier
+// binary32 kernels that were measured slower and removed.
 #define RT_VARIANT_PLANE 0
 #define RT_VARIANT_CELL 1
 #define RT_VARIANT_TMA 2
 #define RT_VARIANT_GROUP 3
-#define RT_VARIANT_PIPE 4
-#define RT_VARIANT_WS 5
-#define RT_VARIANT_WSD 6
-#define RT_VARIANT_W2 7
-#define RT_VARIANT_W2D 8
-#define RT_VARIANT_W3 9
-#define RT_VARIANT_W4 10
-#define RT_VARIANT_W5 11
-#define RT_VARIANT_W5H 12
-#define RT_VARIANT_W6 13
-#define RT_VARIANT_W2Z 14
+#define RT_VARIANT_W3 9       // binary32: every operand staged by TMA
+#define RT_VARIANT_W6 13      // binary32: small planes, z slices per item
+#define RT_VARIANT_W2Z 14     // binary32 production step: 2-wide blocks, z-march
 #define RT_VARIANT_SPLIT 15   // binary64: every face flux once, two passes (rt_split.cu)
 #define RT_VARIANT_FAST 16    // binary64: two passes without divisions (rt_fast.cu), within 1e-12 of the reference
 struct StepTuning {
@@ -136,7 +132,7 @@ int w6_blocks_per_sm(int threads, size_t smem);
 cudaError_t launch_batch_w6(const void* members, const long long* first, int nmem, int threads, int ns,
                             long long stage_floats, int grid, cudaStream_t st);
 // persistent binary32 kernels (dispatch in rt_persist.cu; the families in
-// rt_persist.cu, rt_persist_w2.cu, rt_persist_ws.cu); done = false when the tuning
+// rt_persist.cu, rt_persist_w2.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them
 cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaStream_t st, bool& done);
 // two-pass binary64 step (rt_split.cu): the face fluxes of every axis with

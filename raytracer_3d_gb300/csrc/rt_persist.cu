@@ -2,9 +2,9 @@
 // the dispatch over every persistent variant (launch_persist), the form with
 // every operand staged by TMA (rt_step8.cuh, RT_VARIANT_W3) single-field and
 // batched, and the small-plane form with z slices per item (rt_step11.cuh,
-// RT_VARIANT_W6, also the ensemble class of small planes).  The other
-// families are instantiated in rt_persist_w2.cu and rt_persist_ws.cu so the
-// library builds in parallel.
+// RT_VARIANT_W6, also the ensemble class of small planes).  The production
+// 2-wide z-march kernel is instantiated in rt_persist_w2.cu so the library
+// builds in parallel.
 #include "rt_persist.cuh"
 
 namespace rt {
@@ -209,21 +209,6 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
       return launch_w6_nt<512>(A, S, nullptr, nullptr, 0, nitems, ns, sf, grid, st);
     }
   }
-  if (tn.variant == RT_VARIANT_W5 && w5_ok(A.d, 256, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_w5_family(A, S, 256, tn.threads, st);
-  }
-  if (tn.variant == RT_VARIANT_W5H && w5_ok(A.d, 128, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_w5_family(A, S, 128, tn.threads, st);
-  }
-  if (tn.variant == RT_VARIANT_W4 && w2_ok(A.d, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_w4_family(A, S, tn.threads, st);
-  }
   if (tn.variant == RT_VARIANT_W3 && w3_ok(A.d, tn.threads)) {
     done = true;
     const PlaneSched S = make_sched(A.d, tn);
@@ -235,22 +220,7 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
     done = true;
     // columns of z in band order over (k,l,m): units are k alone (gz = nz)
     const PlaneSched S = make_sched(A.d, tn, A.d.n[2]);
-    return launch_w2_family(A, S, tn.threads, 0, 1, st);
-  }
-  if ((tn.variant == RT_VARIANT_W2 || tn.variant == RT_VARIANT_W2D) && w2_ok(A.d, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_w2_family(A, S, tn.threads, tn.variant == RT_VARIANT_W2 ? 1 : 0, 0, st);
-  }
-  if ((tn.variant == RT_VARIANT_WS || tn.variant == RT_VARIANT_WSD) && ws_ok(A.d, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_ws_family(A, S, tn.threads, tn.variant == RT_VARIANT_WS ? 1 : 0, st);
-  }
-  if (tn.variant == RT_VARIANT_PIPE && pipe_ok(A.d, tn.threads)) {
-    done = true;
-    const PlaneSched S = make_sched(A.d, tn);
-    return launch_pipe_family(A, S, tn.threads, st);
+    return launch_w2z(A, S, tn.threads, st);
   }
   return cudaSuccess;
 }

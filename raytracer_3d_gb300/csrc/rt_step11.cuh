@@ -19,7 +19,7 @@
 // Requires nx, ny multiples of 4 and every axis z..m longer than one.
 // The same kernel steps one field or, over a member list, an ensemble.
 #pragma once
-#include "rt_step10.cuh"
+#include "rt_step8.cuh"
 
 namespace rt {
 

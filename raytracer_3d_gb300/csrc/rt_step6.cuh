@@ -1,8 +1,10 @@
-// rt_step6.cuh -- warp-specialised, multi-stage TMA step (binary32 form).
+// rt_step6.cuh -- the producer side of the warp-specialised binary32 step
+// kernels (rt_step7.cuh, rt_step8.cuh, rt_step11.cuh).
 //
-// Work items are the (z,k) planes of (x,y) at one (l,m) in band order, as in
-// rt_step5.cuh, walked by persistent CTAs (CTA b takes items b, b+G, ...).
-// Each CTA has NT consumer threads and one producer warp:
+// Work items are the (z,k) planes of (x,y) at one (l,m) in band order, or
+// with the z-march whole z columns of one (k,l,m), walked by persistent CTAs
+// (CTA b takes items b, b+G, ...).  Each CTA has NT consumer threads and one
+// producer warp:
 //
 //   producer (one warp): decodes the next items, writes their descriptors
 //     (plane offset, left-face velocity bases, face-0 bases, grid constants)
@@ -10,23 +12,19 @@
 //     a ring of `ns` stages (2..4, as many as fit).  Stage s is refilled only
 //     after every consumer thread has released it (mbarrier empty[s]);
 //     copies complete on full[s]; descriptors are published on dful[s].
-//   consumers: thread t owns column x = t % nx and R consecutive rows
-//     y0 = (t / nx) * R ...; it loads its velocities and growth rate of the
-//     NEXT item into registers while it computes the current one.
-//     x-face fluxes are computed once per face and passed to the right
-//     neighbour with a warp shuffle (the first lane of a warp whose column is
-//     not 0 computes its left face itself); y-face fluxes are computed once
-//     per face inside the thread's rows, plus the face below the first row.
+//   consumers: the kernels of the files named above.
 //
 // No CTA-wide barrier runs inside the item loop: warps drift by up to `ns`
-// items.  Every mbarrier wait is bounded (status bit 0, no hang).  The
-// arithmetic (flux_fp32, axis order x,y,z,k,l,m, divergence and update
-// expressions) is that of the other binary32 step kernels: results are
-// bit-identical to them.
+// items.  Every mbarrier wait is bounded (status bit 0, no hang).
 #pragma once
-#include "rt_step5.cuh"
+#include "rt_step3.cuh"
 
 namespace rt {
+
+// work items of the plane schedule: one (z,k,l,m) plane of (x,y) each
+__host__ __device__ __forceinline__ long long dense_items(const Dims& d) {
+  return (long long)d.n[2] * d.n[3] * d.n[4] * d.n[5];
+}
 
 #define RT_WS_MAXSTAGE 4
 
@@ -247,190 +245,6 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
     if (uses == 0) continue;
     for (uint32_t w = 0; w < RT_WAIT_LIMIT; w++)
       if (mbar_try_wait(&full[j], (uint32_t)((uses - 1) & 1))) break;
-  }
-}
-
-// a consumer thread's per-item values
-template <int R>
-struct WsRegs {
-  float vx[R], vy[R], vr[4][R], vl[4][R], lam[R];
-  float xl[R];   // x == 0: face-0 velocity; first lane with x > 0: velocity of face x
-  float yb;      // y0 == 0: face-0 velocity; else velocity of face y0 (below row y0)
-};
-
-template <int R>
-__device__ __forceinline__ void ws_load(const StepArgs<float>& A, const WsDesc& D, int x, int y0,
-                                        const int yrow[R], int lane, WsRegs<R>& G) {
-  const Dims& d = A.d;
-  const int nx = d.n[0], ny = d.n[1];
-  const long long p0 = D.p0;
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    const int q = yrow[r] * nx + x;
-    const long long o = p0 + q;
-    G.vx[r] = ld_stream(A.vel[0] + o);
-    G.vy[r] = ld_stream(A.vel[1] + o);
-#pragma unroll
-    for (int a = 2; a < 6; a++) {
-      const bool act = d.n[a] > 1;
-      G.vr[a - 2][r] = act ? A.vel[a][o] : 0.f;
-      G.vl[a - 2][r] = act ? D.vl[a - 2][q] : 0.f;
-    }
-    G.lam[r] = ld_stream(A.lam[0] + o);
-    G.xl[r] = x == 0 ? D.b0x[yrow[r]] : (lane == 0 ? A.vel[0][o - 1] : 0.f);
-  }
-  G.yb = y0 == 0 ? D.b0y[x] : (y0 < ny ? A.vel[1][p0 + (long long)(y0 - 1) * nx + x] : 0.f);
-}
-
-template <int NT, int R>
-struct WsMinBlocks { static constexpr int value = (NT <= 256 && R <= 2) ? 2 : 1; };
-
-// PF = 1: the next item's velocities are loaded into registers while the
-// current item is computed; PF = 0: they are loaded at the start of the item
-// (fewer registers; the other warps cover the latency)
-template <int NT, int R, int PF>
-__global__ void __launch_bounds__(NT + 32, (WsMinBlocks<NT, R>::value))
-    step_ws_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
-  uint64_t* empty = full + RT_WS_MAXSTAGE;
-  uint64_t* dful = empty + RT_WS_MAXSTAGE;
-  WsDesc* desc = reinterpret_cast<WsDesc*>(smem_raw + 128);
-  float* stage0 = reinterpret_cast<float*>(smem_raw + ws_head_bytes());
-  const Dims& d = A.d;
-  const int nx = d.n[0], ny = d.n[1], nxy = nx * ny;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < ns; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], NT);
-      mbar_init(&dful[s], 1);
-    }
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (blockIdx.x >= nitems) return;
-
-  if (threadIdx.x >= NT) {
-    ws_produce(A, S, nitems, ns, full, empty, dful, desc, stage0);
-    return;
-  }
-
-  // ---- consumer: the thread's column and rows, fixed for every item ----
-  const int t = threadIdx.x, lane = t & 31;
-  const int x = t % nx, y0 = (t / nx) * R;
-  int yrow[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) yrow[r] = y0 + r < ny ? y0 + r : ny - 1;
-  const int xm = x > 0 ? x - 1 : 0, xp = x + 1 < nx ? x + 1 : nx - 1, xpp = x + 2 < nx ? x + 2 : nx - 1,
-            xmm = x > 1 ? x - 2 : 0;
-  const float cx = A.t32.hcfl[0][pidx(x + 1)], ix = A.t32.inv_d[0][pidx(x + 1)];
-  const float cxl = A.t32.hcfl[0][pidx(x)];
-  float cy[R], iy[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
-    iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
-  }
-  const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
-  // smem offsets of the column's rows y0-2 .. y0+R+1 (clamped)
-  int ecol[R + 4];
-#pragma unroll
-  for (int j = 0; j < R + 4; j++) {
-    int yy = y0 + j - 2;
-    yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
-    ecol[j] = yy * nx + x;
-  }
-  const float dt = (float)A.dt;
-
-  WsRegs<R> cur, nxt;
-  if (PF) {
-    if (!ws_wait(&dful[0], 0, A.status)) return;
-    ws_load<R>(A, desc[0], x, y0, yrow, lane, cur);
-  }
-
-  int s = 0;
-  uint32_t par = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
-    int sn = s + 1;
-    uint32_t parn = par;
-    if (sn == ns) { sn = 0; parn ^= 1u; }
-    if (PF) {
-      // ---- look ahead: the next item's registers ----
-      if (it + gridDim.x < nitems) {
-        if (!ws_wait(&dful[sn], parn, A.status)) return;
-        ws_load<R>(A, desc[sn], x, y0, yrow, lane, nxt);
-      }
-    } else {
-      if (!ws_wait(&dful[s], par, A.status)) return;
-      ws_load<R>(A, desc[s], x, y0, yrow, lane, cur);
-    }
-    const WsDesc& D = desc[s];
-    const long long p0 = D.p0;
-    float kcr[4], kir[4], kcl[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      kcr[a] = D.kcfl_r[a];
-      kir[a] = D.kinv_r[a];
-      kcl[a] = D.kcfl_l[a];
-    }
-    if (!ws_wait(&full[s], par, A.status)) return;
-    const float* sE = stage0 + (size_t)s * RT_NPLANE * nxy;
-
-    float ec[R + 4];
-#pragma unroll
-    for (int j = 0; j < R + 4; j++) ec[j] = sE[ecol[j]];
-    // ---- x faces: right face here, left face from the lane to the left ----
-    float fxr[R], fxl[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const int rb = yrow[r] * nx;
-      fxr[r] = flux_fp32(cur.vx[r], cx, sE[rb + xm], ec[r + 2], sE[rb + xp], sE[rb + xpp]);
-    }
-#pragma unroll
-    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxr[r], 1);
-    if (x == 0) {
-#pragma unroll
-      for (int r = 0; r < R; r++) fxl[r] = open_face0_flux<float>(cur.xl[r], ec[r + 2]);
-    } else if (lane == 0) {
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        const int rb = yrow[r] * nx;
-        fxl[r] = flux_fp32(cur.xl[r], cxl, sE[rb + xmm], sE[rb + x - 1], ec[r + 2], sE[rb + xp]);
-      }
-    }
-    // ---- y faces: below the first row, then above every row ----
-    float fy[R + 1];
-    fy[0] = y0 == 0 ? open_face0_flux<float>(cur.yb, ec[2])
-                    : flux_fp32(cur.yb, cyb, ec[0], ec[1], ec[2], ec[3]);
-#pragma unroll
-    for (int r = 0; r < R; r++) fy[r + 1] = flux_fp32(cur.vy[r], cy[r], ec[r + 1], ec[r + 2], ec[r + 3], ec[r + 4]);
-    // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const float e0 = ec[r + 2];
-      const int q = yrow[r] * nx + x;
-      float dE = 0.f;
-      dE -= (fxr[r] - fxl[r]) * ix;
-      dE -= (fy[r + 1] - fy[r]) * iy[r];
-#pragma unroll
-      for (int a = 2; a < 6; a++) {
-        if (d.n[a] <= 1) continue;
-        const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
-        const float Em2 = sN[0], Em1 = sN[nxy], Ep1 = sN[2 * nxy], Ep2 = sN[3 * nxy];
-        const float fr = flux_fp32(cur.vr[a - 2][r], kcr[a - 2], Em1, e0, Ep1, Ep2);
-        const float fl = flux_fp32(cur.vl[a - 2][r], kcl[a - 2], Em2, Em1, e0, Ep1);
-        dE -= (fr - fl) * kir[a - 2];
-      }
-      const float mf = e0 * cur.lam[r];
-      if (y0 + r < ny) st_stream(A.Enew + p0 + q, e0 + dt * (dE - mf));
-    }
-    // ---- release the stage: this thread's reads of it and of its
-    // descriptor are done (every consumer thread arrives) ----
-    mbar_arrive(&empty[s]);
-    if (PF) cur = nxt;
-    s = sn;
-    par = parn;
   }
 }
 

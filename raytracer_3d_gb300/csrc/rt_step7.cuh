@@ -1,7 +1,12 @@
-// rt_step7.cuh -- warp-specialised multi-stage step with 2-wide cell blocks
-// (binary32 form).
+// rt_step7.cuh -- the production binary32 step: warp-specialised, multi-stage,
+// 2-wide cell blocks, CTAs marching along z.
 //
-// Same producer, stage ring, descriptors and item order as rt_step6.cuh.
+// Producer, stage ring and descriptors are those of rt_step6.cuh; each CTA
+// walks whole z columns of one (k,l,m) (columns in band order over (k,l,m)),
+// so the flux a cell computes on its right z face is its left z-face flux on
+// the next plane (same inputs: carried in a register, bit-identical), and
+// neither the left z velocities nor the z-2 plane are fetched after a
+// column's first plane.
 // A consumer thread owns a block of 2 (x) by R (y) cells: columns
 // x0 = 2*(t % (nx/2)), x0+1 and rows y0 = (t / (nx/2))*R ... y0+R-1, so
 // every shared-memory and global access of the block is an 8-byte pair.
@@ -56,16 +61,11 @@ __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& 
                  : (y0 < ny ? ld2(A.vel[1] + p0 + (long long)(y0 - 1) * nx + x0) : make_float2(0.f, 0.f));
 }
 
+// nitems counts the (k,l,m) columns; the walk (ItemWalk) visits z = 0..nz-1
+// of each
 template <int NT, int R>
-struct W2MinBlocks { static constexpr int value = 1; };
-
-// ZM = 1: z-march (ItemWalk): the CTA walks whole z columns, so the flux a
-// cell computes on its right z face is the next item's left z face flux of
-// the same cell (same inputs: the value is carried, bit-identical).
-// nitems counts columns then.
-template <int NT, int R, int PF, int ZM = 0>
-__global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
-    step_w2_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
+__global__ void __launch_bounds__(NT + 32, 1)
+    step_w2z_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
   uint64_t* empty = full + RT_WS_MAXSTAGE;
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
   if (blockIdx.x >= nitems) return;
 
   if (threadIdx.x >= NT) {
-    ws_produce<ZM != 0>(A, S, nitems, ns, full, empty, dful, desc, stage0);
+    ws_produce<true>(A, S, nitems, ns, full, empty, dful, desc, stage0);
     return;
   }
 
@@ -120,31 +120,17 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
   }
   const float dt = (float)A.dt;
 
-  W2Regs<R> cur, nxt;
-  if (PF) {
-    if (!ws_wait(&dful[0], 0, A.status)) return;
-    w2_load<R>(A, desc[0], x0, y0, yrow, lane, cur);
-  }
-
+  W2Regs<R> cur;
   int s = 0;
   uint32_t par = 0;
-  float2 zcarry[R];   // z-march: the right z face flux of the previous item, per row
-  ItemWalk<ZM != 0> wk;
+  float2 zcarry[R];   // the right z face flux of the previous plane of the column, per row
+  ItemWalk<true> wk;
   for (wk.start(); wk.valid(nitems); wk.next(d.n[2])) {
     int sn = s + 1;
     uint32_t parn = par;
     if (sn == ns) { sn = 0; parn ^= 1u; }
-    if (PF) {
-      ItemWalk<ZM != 0> wn = wk;
-      wn.next(d.n[2]);
-      if (wn.valid(nitems)) {
-        if (!ws_wait(&dful[sn], parn, A.status)) return;
-        w2_load<R>(A, desc[sn], x0, y0, yrow, lane, nxt);
-      }
-    } else {
-      if (!ws_wait(&dful[s], par, A.status)) return;
-      w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur, ZM && wk.z > 0);
-    }
+    if (!ws_wait(&dful[s], par, A.status)) return;
+    w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur, wk.z > 0);
     const WsDesc& D = desc[s];
     const long long p0 = D.p0;
     float kcr[4], kir[4], kcl[4];
@@ -216,7 +202,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
         const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
         const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
         float fla, flb;
-        if (ZM && a == 2 && wk.z > 0) {   // left z face = the previous plane's right z face
+        if (a == 2 && wk.z > 0) {   // left z face = the previous plane's right z face
           fla = zcarry[r].x;
           flb = zcarry[r].y;
         } else {
@@ -224,7 +210,7 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
           fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
           flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
         }
-        if (ZM && a == 2) zcarry[r] = make_float2(fra, frb);
+        if (a == 2) zcarry[r] = make_float2(fra, frb);
         dEa -= (fra - fla) * kir[a - 2];
         dEb -= (frb - flb) * kir[a - 2];
       }
@@ -232,7 +218,6 @@ __global__ void __launch_bounds__(NT + 32, (W2MinBlocks<NT, R>::value))
       if (y0 + r < ny) st2_stream(A.Enew + p0 + q, make_float2(e0.x + dt * (dEa - mfa), e0.y + dt * (dEb - mfb)));
     }
     mbar_arrive(&empty[s]);
-    if (PF) cur = nxt;
     s = sn;
     par = parn;
   }

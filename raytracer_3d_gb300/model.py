@@ -259,7 +259,8 @@ class Model:
         return {k: getattr(b, k) for k in _lib.BUDGET_FIELDS}, arrs
 
     # ---- plumbing ---------------------------------------------------------------
-    VARIANTS = {"plane": 0, "cell": 1, "tma": 2, "group": 3, "pipe": 4, "ws": 5, "wsd": 6, "w2": 7, "w2d": 8, "w3": 9, "w4": 10, "w5": 11, "w5h": 12, "w6": 13, "w2z": 14, "split": 15, "fast": 16}
+    # rt_set_tuning codes (4-8 and 10-12 belonged to removed binary32 kernels)
+    VARIANTS = {"plane": 0, "cell": 1, "tma": 2, "group": 3, "w3": 9, "w6": 13, "w2z": 14, "split": 15, "fast": 16}
 
     def set_tuning(self, variant="tma", band=8, threads=512, sweep=0):
         """Schedule of the step kernel; never changes results."""

@@ -71,12 +71,8 @@ def test_coefficients_bit_identical(name):
 
 SCHEDULES = [("tma", 8, 1024, 0), ("tma", 3, 128, 1), ("tma", 1, 512, 0), ("plane", 8, 256, 0),
              ("plane", 2, 512, 1), ("group", 8, 256, 0), ("group", 3, 1024, 1), ("group", 2, 128, 0),
-             ("pipe", 8, 256, 0), ("pipe", 3, 512, 1), ("pipe", 5, 1024, 0), ("ws", 8, 256, 0),
-             ("ws", 3, 512, 1), ("wsd", 4, 128, 0), ("wsd", 8, 512, 1), ("w2", 8, 256, 0), ("w2", 3, 512, 1),
-             ("w2d", 4, 128, 0), ("w2d", 8, 256, 1), ("w3", 8, 256, 0), ("w3", 3, 512, 1),
-             ("w3", 4, 128, 0), ("w4", 8, 512, 0), ("w4", 3, 256, 1), ("w4", 4, 128, 0), ("w5", 8, 512, 0),
-             ("w5", 3, 256, 1), ("w5h", 4, 512, 0), ("w5h", 8, 256, 1), ("w6", 8, 256, 0), ("w6", 3, 512, 1),
-             ("w2z", 8, 512, 1), ("w2z", 3, 256, 0), ("cell", 8, 256, 0), ("split", 8, 256, 0)]
+             ("w3", 8, 256, 0), ("w3", 3, 512, 1), ("w3", 4, 128, 0), ("w6", 8, 256, 0), ("w6", 3, 512, 1),
+             ("w2z", 8, 512, 1), ("w2z", 3, 256, 0), ("w2z", 4, 128, 0), ("cell", 8, 256, 0), ("split", 8, 256, 0)]
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -185,10 +181,13 @@ def test_config1_packet_200_steps():
         b, _ = exact.diagnose(fields=False)
         bf, _ = fast.diagnose(fields=False)
         bo = o.diagnose()
+        # the sums run over 4.2 M cells in another order than the oracle's
+        # sequential loops: compared to 1e-13 of the budget's scale (the
+        # z-end boundary flux, for one, nearly cancels under reflection)
         sums = [k for k in bo if k in ("eint", "mflint") or k.startswith("bfl")]
         scale = sum(abs(bo[k]) for k in sums)
         for k in sums:
-            assert abs(b[k] - bo[k]) <= 1e-12 * max(abs(bo[k]), 1e-300) + 1e-15 * scale, (k, b[k], bo[k])
+            assert abs(b[k] - bo[k]) <= 1e-12 * max(abs(bo[k]), 1e-300) + 1e-13 * scale, (k, b[k], bo[k])
         assert abs(b["residual"]) <= 1e-12 * scale
         assert abs(bf["residual"]) <= 1e-12 * scale
         e_ref = float(np.sum(o.E[sl] * vol))
@@ -319,16 +318,8 @@ def test_fp32_schedules_agree():
 
 @pytest.mark.parametrize("n", [(32, 32, 4, 4, 2, 6), (24, 16, 6, 4, 6, 10), (16, 8, 5, 2, 4, 6),
                                (20, 12, 4, 2, 4, 6), (64, 64, 4, 2, 2, 2)])
-@pytest.mark.parametrize("tuning", [("pipe", 4, 256, 0), ("pipe", 4, 512, 1), ("pipe", 8, 1024, 0),
-                                    ("ws", 4, 128, 0), ("ws", 4, 256, 1), ("ws", 8, 512, 0),
-                                    ("wsd", 4, 128, 1), ("wsd", 4, 256, 0), ("wsd", 8, 512, 1),
-                                    ("w2", 4, 128, 0), ("w2", 4, 256, 1), ("w2", 8, 512, 0),
-                                    ("w2d", 4, 128, 1), ("w2d", 4, 256, 0), ("w2d", 8, 512, 1),
-                                    ("w3", 4, 128, 1), ("w3", 4, 256, 0), ("w3", 8, 512, 1),
-                                    ("w4", 4, 128, 1), ("w4", 4, 256, 0), ("w4", 8, 512, 1),
-                                    ("w5", 4, 256, 1), ("w5", 8, 512, 0), ("w5h", 4, 128, 0),
-                                    ("w5h", 4, 256, 1), ("w5h", 8, 512, 0), ("w6", 4, 256, 1),
-                                    ("w6", 8, 512, 0), ("w2z", 4, 256, 1), ("w2z", 8, 512, 0),
+@pytest.mark.parametrize("tuning", [("w3", 4, 128, 1), ("w3", 4, 256, 0), ("w3", 8, 512, 1),
+                                    ("w6", 4, 256, 1), ("w6", 8, 512, 0), ("w2z", 4, 256, 1), ("w2z", 8, 512, 0),
                                     ("w2z", 4, 128, 0)],
                          ids=lambda t: "%s-b%d-t%d-s%d" % t)
 def test_fp32_persistent_matches_tma(n, tuning):
@@ -346,7 +337,7 @@ def test_fp32_persistent_matches_tma(n, tuning):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("variant", ["tma", "group", "plane", "pipe", "ws", "wsd", "w2", "w2d", "w3", "w4", "w5", "w5h", "w6", "w2z", "cell"])
+@pytest.mark.parametrize("variant", ["tma", "group", "plane", "w3", "w6", "w2z", "cell"])
 def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
     after 200 steps of the all-axes shear case."""
@@ -373,7 +364,7 @@ def test_fp32_form_against_fp64_oracle(variant):
         m.close()
 
 
-@pytest.mark.parametrize("variant", ["tma", "group", "w2z", "w3", "w6", "w2d"])
+@pytest.mark.parametrize("variant", ["tma", "group", "w2z", "w3", "w6"])
 def test_fp32_stretched_against_fp64_oracle(variant):
     """binary32 form on non-uniform grids (per-cell 1/d and dt/2d tables):
     error after 100 steps of the stretched all-axes case, 8x8 planes and 256
