@@ -232,7 +232,12 @@ SCHEDULE_NOTES = {
 }
 
 
-def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False, candidates=None):
+def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=False, candidates=None,
+             final_step=0):
+    """time one form on the jet workload; with final_step > 0 the model is
+    then stepped on to exactly final_step steps from the initial state and
+    its interior is returned (out["final"]) for the error against the other
+    precision"""
     import numpy as np
     import torch
     from raytracer_3d_gb300 import configs
@@ -270,11 +275,68 @@ def run_form(precision, n, steps, warmup, dist, e2e_steps, sched=None, tune=Fals
         out["e2e"] = {"seconds": e2e_secs, "steps": e2e_steps,
                       "bytes": cells * 8, "host_access": "direct" if m.host_direct() else "staged"}
         out["finite"] = bool(np.isfinite(m.E).all())
+    if final_step > 0:
+        if m.itt > final_step:
+            raise ValueError("error comparison at step %d, but the form took %d steps" % (final_step, m.itt))
+        out["energy0"] = energy_sum(initial_interior(exp, m), vol_weights(m))
+        m.integrate(final_step - m.itt)
+        sl = tuple(slice(2, 2 + k) for k in m.n)
+        out["final"] = np.array(m.get_state()[sl], dtype=np.float64, order="F")
+        out["widths"] = vol_weights(m)
     m.close()
     return out
 
 
-def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None):
+def vol_weights(model):
+    return [model.grid["xyzklm"[a]]["dt"][2:2 + model.n[a]] for a in range(6)]
+
+
+def initial_interior(exp, model):
+    """the experiment's initial state (interior, binary64), rebuilt from its
+    seed on a stand-in that carries only what the initial conditions read"""
+    import numpy as np
+
+    class Shell:
+        pass
+    shell = Shell()
+    shell.n, shell.padded, shell.grid = model.n, False, model.grid
+    shell.E = np.zeros(model.n, order="F")
+    exp.initial(shell, np.random.Generator(np.random.PCG64(exp.seed)))
+    return shell.E
+
+
+def energy_sum(E, widths):
+    """sum(E*vol) of an interior 6D array, one m plane at a time"""
+    import numpy as np
+    v5 = np.ones([len(w) for w in widths[:5]])
+    for a in range(5):
+        shp = [1] * 5
+        shp[a] = len(widths[a])
+        v5 = v5 * widths[a].reshape(shp)
+    return sum(float(np.sum(np.asarray(E[..., m], dtype=np.float64) * v5)) * float(widths[5][m])
+               for m in range(E.shape[5]))
+
+
+def error_against(got, ref, widths, energy0=None):
+    """relative L2 and L-inf (to max |ref|) of got - ref and the relative
+    total-energy difference, one m plane at a time"""
+    import numpy as np
+    num2 = den2 = dmax = rmax = 0.0
+    for m in range(ref.shape[5]):
+        r = np.asarray(ref[..., m], dtype=np.float64)
+        d = np.asarray(got[..., m], dtype=np.float64) - r
+        num2 += float(np.sum(d * d))
+        den2 += float(np.sum(r * r))
+        dmax = max(dmax, float(np.max(np.abs(d))))
+        rmax = max(rmax, float(np.max(np.abs(r))))
+    e_ref, e_got = energy_sum(ref, widths), energy_sum(got, widths)
+    out = {"l2": (num2 / den2) ** 0.5, "linf": dmax / rmax, "energy": abs(e_got - e_ref) / abs(e_ref)}
+    if energy0:
+        out["reference_energy_change"] = abs(e_ref - energy0) / abs(energy0)
+    return out
+
+
+def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None, error_steps=0):
     """48 independent fp32 instances (dims per axis from {8,16,24,32} spatial
     and {8,12,16,24} spectral, own N0, f, mean-flow amplitude, packet init)
     advanced by one persistent, graph-captured launch per step, with the
@@ -314,42 +376,74 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
     secs = e0.elapsed_time(e1) / 1e3
     b.sync()
     cells = b.cells
+    error = None
+    if error_steps > 0:
+        # every member on to error_steps in the batch, then each alone in
+        # binary64 (the fast schedule) from the same initial state
+        taken = warmup + steps
+        if error_steps > taken:
+            b.integrate(error_steps - taken)
+        b.sync()
+        worst = {"l2": 0.0, "linf": 0.0, "energy": 0.0}
+        for e, m in zip(exps, models):
+            got = m.get_state()
+            r = configs.build_model(e, "fp64", padded=False)
+            r.set_tuning("fast", 8, 256)
+            r.integrate(max(error_steps, taken))
+            err = error_against(got, r.get_state(), vol_weights(r))
+            r.close()
+            for k in worst:
+                worst[k] = max(worst[k], err[k])
+        error = {"steps": max(error_steps, taken), "worst_member": worst,
+                 "reference": "each member alone in binary64 (fast schedule, within 1e-12 per step of the "
+                              "reference's arithmetic)"}
     out = {"value": cells * steps / secs, "unit": UNIT, "members": members, "cells_per_step": cells,
            "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": b.launch_count() - l0,
            "graph_steps": b.tuning[3],
            "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
                       "slice_threads": best[4], "staged_members": b.persistent_members()},
-           "roofline": roofline("fp32", cells, secs / steps), "clocks": cs.summary(),
-           "setup_s": round(setup_s, 2)}
+           "roofline": roofline("fp32", cells, secs / steps, "batch_fp32"), "clocks": cs.summary(),
+           "setup_s": round(setup_s, 2), "error": error}
     b.close()
     for m in models:
         m.close()
     return out
 
 
-def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=2):
+def bench_serving(nreq=60, rate=20.0, seed=77, budget=120e9, baseline_req=12, stable_rate=1.5, stable_req=30,
+                  fp64_schedule=("fast", 8, 256, 0)):
     """Poisson arrivals (mean 20/s), step counts uniform in [50,1000], dims
-    as the batched form, 120 GB HBM budget, fp32 continuous batching; and the
-    fp64 one-at-a-time baseline on the first requests."""
+    as the batched form, 120 GB HBM budget, fp32 continuous batching; the
+    same at an arrival rate the GPU keeps up with; and the fp64
+    one-at-a-time baseline on the first requests of the same trace."""
     from raytracer_3d_gb300.serve import GpuExecutor, SequentialExecutor, Server, poisson_requests
-    reqs = poisson_requests(nreq, rate=rate, seed=seed)
-    ex = GpuExecutor("fp32", batch_tuning=(8, 512, 1, 16), persistent=512)
-    rep = Server(ex, budget_bytes=budget, chunk_max=50, setup_workers=8).run(reqs)
-    ex.close()
-    breakdown = {k: round(v, 2) for k, v in ex.times.items()}
-    breakdown["batch_rebuilds"] = ex.rebuilds
-    s = rep.summary()
-    for r in reqs:
-        r.result = None
-    base = poisson_requests(baseline_req, rate=rate, seed=seed)
-    exb = SequentialExecutor("fp64")
+
+    def serve(reqs):
+        ex = GpuExecutor("fp32", batch_tuning=(8, 512, 1, 16), persistent=512)
+        rep = Server(ex, budget_bytes=budget, chunk_max=50, setup_workers=8).run(reqs)
+        ex.close()
+        breakdown = {k: round(v, 2) for k, v in ex.times.items()}
+        breakdown["batch_rebuilds"] = ex.rebuilds
+        for r in reqs:
+            r.result = None
+        return rep.summary(), breakdown
+
+    s, breakdown = serve(poisson_requests(nreq, rate=rate, seed=seed))
+    st, _ = serve(poisson_requests(stable_req, rate=stable_rate, seed=seed + 1))
+    base = poisson_requests(nreq, rate=rate, seed=seed)[:baseline_req]
+    exb = SequentialExecutor("fp64", schedule=fp64_schedule)
     repb = Server(exb, budget_bytes=budget, chunk_max=10 ** 9, max_members=1).run(base)
     sb = repb.summary()
     return {"requests": nreq, "arrival_rate_per_s": rate, "budget_bytes": budget,
             "p50_s": s["p50_s"], "p99_s": s["p99_s"], "value": s["cell_updates_per_s"], "unit": UNIT,
             "makespan_s": s["makespan_s"], "chunks": s["chunks"], "backlog_max": s["backlog_max"],
             "peak_bytes": s["peak_bytes"], "seconds_by_activity": breakdown,
-            "fp64_one_at_a_time": {"requests": baseline_req, "value": sb["cell_updates_per_s"],
+            "spectral_dims": "each of k, l, m from {8, 12, 16, 24}",
+            "stable_load": {"requests": stable_req, "arrival_rate_per_s": stable_rate, "p50_s": st["p50_s"],
+                            "p99_s": st["p99_s"], "value": st["cell_updates_per_s"],
+                            "makespan_s": st["makespan_s"], "backlog_max": st["backlog_max"]},
+            "fp64_one_at_a_time": {"requests": baseline_req, "trace": "the first requests of the 20/s trace",
+                                   "schedule": fp64_schedule[0], "value": sb["cell_updates_per_s"],
                                    "p50_s": sb["p50_s"], "p99_s": sb["p99_s"]}}
 
 
@@ -405,24 +499,32 @@ def gpu_arm(args):
     # the binary64 form is bound by the FP64 pipe; 256-thread CTAs keep its
     # registers unspilled (the flags set the fp32 schedule when --tune 0)
     peak64 = fp64_peak()
+    err_steps = 0 if args.no_fp32 else args.error_steps
     if args.fp64_variant:
-        main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, (args.fp64_variant, 8, 256, 0))
+        main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, (args.fp64_variant, 8, 256, 0),
+                        final_step=err_steps)
     else:
         main = run_form("fp64", n, args.steps, args.warmup, dist, args.e2e_steps, FP64_CANDIDATES[-1],
-                        tune=args.tune, candidates=FP64_CANDIDATES)
+                        tune=args.tune, candidates=FP64_CANDIDATES, final_step=err_steps)
     f64_sched = tuple(main["schedule"])
     f64_key = {"split": "step_fp64_split", "fast": "step_fp64_fast"}.get(f64_sched[0], "step_fp64")
     forms = {}
     if not args.no_fp32:
-        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune)
-        forms["fp32"] = {"value": f32["cells"] * args.steps * world / f32["seconds"],
+        f32 = run_form("fp32", n, args.steps, args.warmup, dist, 0, sched, tune=args.tune, final_step=err_steps)
+        error = None
+        if err_steps:
+            error = error_against(f32.pop("final"), main["final"], main["widths"], main.get("energy0"))
+            error.update({"steps": err_steps, "reference": "the binary64 run of this bench line (schedule %s) "
+                          "from the same initial state" % f64_sched[0]})
+        forms["fp32"] = {"value": f32["cells"] * args.steps * world / f32["seconds"], "error": error,
                          "ms_per_step": 1e3 * f32["seconds"] / args.steps,
                          "schedule": "%s band %d threads %d sweep %d" % tuple(f32["schedule"]),
                          "tuning_table_ms": f32["tuning_table_ms"],
                          "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
                          "clocks": f32["clocks"]}
     if not args.no_batch:
-        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup, members=args.batch_members)
+        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,
+                                              error_steps=args.batch_error_steps)
     if not args.no_serve:
         forms["serving"] = bench_serving(nreq=args.serve_requests)
     cells = main["cells"]
@@ -508,6 +610,10 @@ def main():
     ap.add_argument("--only", default="all", choices=("all", "batch", "serve"),
                     help="batch / serve: that form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--error-steps", type=int, default=1000,
+                    help="binary32 error against binary64 after this many steps (0: skip)")
+    ap.add_argument("--batch-error-steps", type=int, default=500,
+                    help="ensemble error against binary64 members after this many steps (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -36,8 +36,8 @@ struct rt_handle {
   int elem = 8;                 // bytes per state/coefficient element
   double* grid = nullptr;       // 9 padded 1D arrays
   long long goff[9]{};
-  float* tab32 = nullptr;       // 12 padded 1D arrays
-  long long toff[12]{};
+  float* tab32 = nullptr;       // 24 padded 1D arrays (Tab32)
+  long long toff[24]{};
   double* bg = nullptr;         // 3 padded 3D arrays
   long long bglen = 0;
   void* vel[6]{};
@@ -205,6 +205,8 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   for (int a = 0; a < 6; a++) {
     A.t32.inv_d[a] = h->tab32 + h->toff[a];
     A.t32.hcfl[a] = h->tab32 + h->toff[6 + a];
+    A.t32.chi[a] = h->tab32 + h->toff[12 + a];
+    A.t32.clo[a] = h->tab32 + h->toff[18 + a];
     A.vel[a] = (const T*)h->vel[a];
     A.vlo[a] = (const T*)h->vlo[a];
   }
@@ -216,6 +218,8 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   A.E = (const T*)h->E[src];
   A.Enew = (T*)h->E[1 - src];
   A.dt = h->p.dt;
+  A.dthi = (float)h->p.dt;
+  A.dtlo = (float)(h->p.dt - (double)A.dthi);
   A.status = h->status;
   return A;
 }
@@ -318,16 +322,21 @@ static int refresh_ucfl(rt_handle* h) {
   return RT_OK;
 }
 
-// binary32 tables 1/d and dt/(2d) on the padded range
+// binary32 tables on the padded range: 1/d, dt/(2d), and dt/d as the
+// two-term sum chi + clo
 static int upload_tab32(rt_handle* h) {
   std::vector<double> hg(h->goff[8] + padded_len(h->d, 5));
   CUDA_TRY(h, cudaMemcpy(hg.data(), h->grid, hg.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  std::vector<float> t(h->toff[11] + padded_len(h->d, 5));
+  std::vector<float> t(h->toff[23] + padded_len(h->d, 5));
   for (int a = 0; a < 6; a++)
     for (long long i = 0; i < padded_len(h->d, a); i++) {
       const double dd = hg[h->goff[a] + i];
       t[h->toff[a] + i] = (float)(1.0 / dd);
       t[h->toff[6 + a] + i] = (float)(0.5 * h->p.dt / dd);
+      const double c = h->p.dt / dd;
+      const float chi = (float)c;
+      t[h->toff[12 + a] + i] = chi;
+      t[h->toff[18 + a] + i] = (float)(c - (double)chi);
     }
   CUDA_TRY(h, cudaMemcpy(h->tab32, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice));
   return RT_OK;
@@ -923,7 +932,7 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
   for (int a = 0; a < 6; a++) { h->goff[a] = gl; gl += padded_len(d, a); }
   for (int c = 0; c < 3; c++) { h->goff[6 + c] = gl; gl += padded_len(d, 3 + c); }
   long long tl = 0;
-  for (int k = 0; k < 12; k++) { h->toff[k] = tl; tl += padded_len(d, k % 6); }
+  for (int k = 0; k < 24; k++) { h->toff[k] = tl; tl += padded_len(d, k % 6); }
   h->bglen = padded_len(d, 0) * padded_len(d, 1) * padded_len(d, 2);
   int rc;
   if ((rc = dev_alloc(h, (void**)&h->grid, gl * sizeof(double)))) return bail(rc);

@@ -185,8 +185,12 @@ __global__ void __launch_bounds__(256) step_kernel(StepArgs<T> A) {
     decode(A.d, v3, sp, c);
     const long long p = v3 + sp * A.d.nvol3;
     const T e0 = A.E[p];
-    const CellTerms<T> t = cell_terms<T>(A, p, c, e0);
-    A.Enew[p] = update<T>(e0, t.dE, t.meanfl, A.dt);
+    if constexpr (sizeof(T) == 4) {
+      A.Enew[p] = cell_step32(A, p, c, e0);
+    } else {
+      const CellTerms<T> t = cell_terms<T>(A, p, c, e0);
+      A.Enew[p] = update<T>(e0, t.dE, t.meanfl, A.dt);
+    }
   }
 }
 

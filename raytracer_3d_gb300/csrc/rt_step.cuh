@@ -71,12 +71,33 @@ __device__ __forceinline__ float flux_fp32(float v, float hcfl, float Ea, float 
   return fmaf(h, psi, v * Eu);
 }
 
-// Per-axis small tables of the binary32 form: 1/d(f) and dt/(2 d(f)) on
-// the padded index range (Fortran index f at position f+1).
+// Per-axis small tables of the binary32 form on the padded index range
+// (Fortran index f at position f+1): 1/d(f) (the budget's divergence),
+// dt/(2 d(f)) (the flux), and dt/d(f) as the unevaluated sum chi + clo of
+// two binary32 numbers (the step's divergence).
 struct Tab32 {
   const float* inv_d[6];
   const float* hcfl[6];
+  const float* chi[6];
+  const float* clo[6];
 };
+
+// Divergence and update of the binary32 step.  The step accumulates
+// acc = dt * sum_a (F_l - F_r)/d_a and stores E + acc - dt*E*lambda.  The
+// constants dt/d_a and dt are carried as two-term binary32 sums (about 48
+// bits): a single rounded binary32 constant would scale every flux of an
+// axis alike, so the energy leaving through the open boundaries -- the only
+// fluxes that do not cancel in the total -- and the mean-flow exchange would
+// carry one systematic relative error of up to 2^-24 over a whole run.  With
+// the two-term constants the remaining rounding errors are unbiased and
+// average out in the total energy.
+__device__ __forceinline__ float div32(float acc, float fr, float fl, float chi, float clo) {
+  const float df = fl - fr;
+  return fmaf(df, chi, fmaf(df, clo, acc));
+}
+__device__ __forceinline__ float upd32(float e0, float acc, float mf, float dthi, float dtlo) {
+  return e0 + fmaf(-mf, dthi, fmaf(-mf, dtlo, acc));
+}
 
 template <class T>
 struct StepArgs {
@@ -91,6 +112,7 @@ struct StepArgs {
   const T* uc[6];      // fp64: cached |v*dt/d| of the right faces (fp32: unused)
   const T* ucl[6];     // fp64: the same on the face-0 planes
   double dt;
+  float dthi, dtlo;    // binary32 form: dt as the two-term sum dthi + dtlo
   int* status;         // device flag: bit 0 = a bounded wait timed out
 };
 
@@ -176,6 +198,29 @@ __device__ __forceinline__ CellTerms<float> cell_terms<float>(const StepArgs<flo
   }
   const float mf = e0 * A.lam[0][p];
   return {dE, mf};
+}
+
+// the binary32 step of one cell (the one-thread-per-cell kernel): the same
+// fluxes as cell_terms<float>, the step's divergence and update
+__device__ __forceinline__ float cell_step32(const StepArgs<float>& A, long long p, const int c[6], float e0) {
+  const Dims& d = A.d;
+  float acc = 0.f;
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    if (d.n[a] <= 1) continue;
+    const int ca = c[a];
+    const float Em2 = A.E[nb_index(d, p, a, ca, -2, c[5])];
+    const float Em1 = A.E[nb_index(d, p, a, ca, -1, c[5])];
+    const float Ep1 = A.E[nb_index(d, p, a, ca, +1, c[5])];
+    const float Ep2 = A.E[nb_index(d, p, a, ca, +2, c[5])];
+    const int F = ca + 1;
+    const float vr = A.vel[a][p];
+    const float vl = ca > 0 ? A.vel[a][p - d.s[a]] : A.vlo[a][plane_index(d, a, c)];
+    const float fr = flux_fp32(vr, A.t32.hcfl[a][pidx(F)], Em1, e0, Ep1, Ep2);
+    const float fl = flux_fp32(vl, A.t32.hcfl[a][pidx(F - 1)], Em2, Em1, e0, Ep1);
+    acc = div32(acc, fr, fl, A.t32.chi[a][pidx(F)], A.t32.clo[a][pidx(F)]);
+  }
+  return upd32(e0, acc, e0 * A.lam[0][p], A.dthi, A.dtlo);
 }
 
 }  // namespace rt

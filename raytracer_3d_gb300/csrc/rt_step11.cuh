@@ -28,8 +28,9 @@ namespace rt {
 struct W6Desc {
   long long p0;   // cell (0,0) of slice z0
   int member, z0;
-  float kr[4], ki[4], kl[4];                              // k,l,m faces (index a-2)
-  float zr[RT_W6_MAXG], zi[RT_W6_MAXG], zl[RT_W6_MAXG];  // z faces of every slice
+  // dt/(2d) of the right face, dt/d of the cell as hi + lo, dt/(2d) of the left face
+  float kr[4], kh[4], ko[4], kl[4];                                    // k,l,m faces (index a-2)
+  float zr[RT_W6_MAXG], zh[RT_W6_MAXG], zo[RT_W6_MAXG], zl[RT_W6_MAXG];  // z faces of every slice
 };
 __host__ __device__ constexpr size_t w6_desc_bytes() { return (sizeof(W6Desc) + 15) / 16 * 16; }
 // the producer's shared-memory copy of the current member's arguments
@@ -175,7 +176,7 @@ struct W6Prep {
   const float* src;   // null: no copy on this lane
   int dst;
   unsigned bytes, tx;
-  float c0, c1, c2;   // this lane's descriptor constants
+  float c0, c1, c3, c2;   // this lane's descriptor constants
 };
 __device__ __forceinline__ W6Prep w6_prepare(const StepArgs<float>& A, const PlaneSched& S, long long li) {
   const Dims& d = A.d;
@@ -191,16 +192,18 @@ __device__ __forceinline__ W6Prep w6_prepare(const StepArgs<float>& A, const Pla
   W6Prep P;
   P.p0 = p0;
   P.z0 = z0;
-  P.c0 = P.c1 = P.c2 = 0.f;
+  P.c0 = P.c1 = P.c3 = P.c2 = 0.f;
   if (lane < G) {
     const int z = z0 + lane < nz ? z0 + lane : nz - 1;
     P.c0 = A.t32.hcfl[2][pidx(z + 1)];
-    P.c1 = A.t32.inv_d[2][pidx(z + 1)];
+    P.c1 = A.t32.chi[2][pidx(z + 1)];
+    P.c3 = A.t32.clo[2][pidx(z + 1)];
     P.c2 = A.t32.hcfl[2][pidx(z)];
   } else if (lane >= 16 && lane < 19) {
     const int a = lane - 13;
     P.c0 = A.t32.hcfl[a][pidx(c[a] + 1)];
-    P.c1 = A.t32.inv_d[a][pidx(c[a] + 1)];
+    P.c1 = A.t32.chi[a][pidx(c[a] + 1)];
+    P.c3 = A.t32.clo[a][pidx(c[a] + 1)];
     P.c2 = A.t32.hcfl[a][pidx(c[a])];
   }
   const W6Copy cp = w6_copy(L, lane, z0, nz);
@@ -259,11 +262,13 @@ __device__ __forceinline__ void w6_commit(const W6Prep& P, int G, int member, fl
   const int lane = threadIdx.x & 31;
   if (lane < G) {
     D->zr[lane] = P.c0;
-    D->zi[lane] = P.c1;
+    D->zh[lane] = P.c1;
+    D->zo[lane] = P.c3;
     D->zl[lane] = P.c2;
   } else if (lane >= 16 && lane < 19) {
     D->kr[lane - 15] = P.c0;   // axis a = lane - 13 at index a - 2
-    D->ki[lane - 15] = P.c1;
+    D->kh[lane - 15] = P.c1;
+    D->ko[lane - 15] = P.c3;
     D->kl[lane - 15] = P.c2;
   }
   if (lane == 0) {
@@ -287,7 +292,7 @@ __device__ __forceinline__ void w6_commit(const W6Prep& P, int G, int member, fl
 struct W6Geom {
   int nx, ny, P, G, g, y, x0, xm, xmm;
   bool has_right, active;
-  float cxa, cxb, ixa, ixb, cxl, cy, iy, cyb, dt;
+  float cxa, cxb, hxa, hxb, oxa, oxb, cxl, cy, hy, oy, cyb, dthi, dtlo;
 };
 
 __device__ __forceinline__ void w6_geom(const StepArgs<float>& A, int G, int t, W6Geom& w) {
@@ -310,13 +315,17 @@ __device__ __forceinline__ void w6_geom(const StepArgs<float>& A, int G, int t, 
   w.has_right = x0 + 2 < nx;
   w.cxa = A.t32.hcfl[0][pidx(x0 + 1)];
   w.cxb = A.t32.hcfl[0][pidx(x0 + 2)];
-  w.ixa = A.t32.inv_d[0][pidx(x0 + 1)];
-  w.ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  w.hxa = A.t32.chi[0][pidx(x0 + 1)];
+  w.hxb = A.t32.chi[0][pidx(x0 + 2)];
+  w.oxa = A.t32.clo[0][pidx(x0 + 1)];
+  w.oxb = A.t32.clo[0][pidx(x0 + 2)];
   w.cxl = A.t32.hcfl[0][pidx(x0)];
   w.cy = A.t32.hcfl[1][pidx(y + 1)];
-  w.iy = A.t32.inv_d[1][pidx(y + 1)];
+  w.hy = A.t32.chi[1][pidx(y + 1)];
+  w.oy = A.t32.clo[1][pidx(y + 1)];
   w.cyb = A.t32.hcfl[1][pidx(y)];
-  w.dt = (float)A.dt;
+  w.dthi = A.dthi;
+  w.dtlo = A.dtlo;
 }
 
 __device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& w, const W6Desc& D,
@@ -363,41 +372,40 @@ __device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& 
   }
   // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
   const float2 e0 = e01;
-  float dEa = 0.f, dEb = 0.f;
-  dEa -= (fxa - fxl) * w.ixa;
-  dEb -= (fxb - fxa) * w.ixb;
-  dEa -= (fyt.x - fyb.x) * w.iy;
-  dEb -= (fyt.y - fyb.y) * w.iy;
+  float dEa = div32(0.f, fxa, fxl, w.hxa, w.oxa);
+  float dEb = div32(0.f, fxb, fxa, w.hxb, w.oxb);
+  dEa = div32(dEa, fyt.x, fyb.x, w.hy, w.oy);
+  dEb = div32(dEb, fyt.y, fyb.y, w.hy, w.oy);
   {
     const float2 Em2 = ld2(sP + L.ez(g) + q), Em1 = ld2(sP + L.ez(g + 1) + q);
     const float2 Ep1 = ld2(sP + L.ez(g + 3) + q), Ep2 = ld2(sP + L.ez(g + 4) + q);
     const float2 vr = ld2(sP + L.v(g, 2) + q), vl = ld2(sP + L.v(g, 6) + q);
-    const float cr = D.zr[g], ci = D.zi[g], cl = D.zl[g];
+    const float cr = D.zr[g], ch = D.zh[g], co = D.zo[g], cl = D.zl[g];
     const float fra = flux_fp32(vr.x, cr, Em1.x, e0.x, Ep1.x, Ep2.x);
     const float fla = flux_fp32(vl.x, cl, Em2.x, Em1.x, e0.x, Ep1.x);
-    dEa -= (fra - fla) * ci;
+    dEa = div32(dEa, fra, fla, ch, co);
     const float frb = flux_fp32(vr.y, cr, Em1.y, e0.y, Ep1.y, Ep2.y);
     const float flb = flux_fp32(vl.y, cl, Em2.y, Em1.y, e0.y, Ep1.y);
-    dEb -= (frb - flb) * ci;
+    dEb = div32(dEb, frb, flb, ch, co);
   }
 #pragma unroll
   for (int a = 3; a < 6; a++) {
     const float2 Em2 = ld2(sP + L.en(g, a, 0) + q), Em1 = ld2(sP + L.en(g, a, 1) + q);
     const float2 Ep1 = ld2(sP + L.en(g, a, 2) + q), Ep2 = ld2(sP + L.en(g, a, 3) + q);
     const float2 vr = ld2(sP + L.v(g, a) + q), vl = ld2(sP + L.v(g, a + 4) + q);
-    const float cr = D.kr[a - 2], ci = D.ki[a - 2], cl = D.kl[a - 2];
+    const float cr = D.kr[a - 2], ch = D.kh[a - 2], co = D.ko[a - 2], cl = D.kl[a - 2];
     const float fra = flux_fp32(vr.x, cr, Em1.x, e0.x, Ep1.x, Ep2.x);
     const float fla = flux_fp32(vl.x, cl, Em2.x, Em1.x, e0.x, Ep1.x);
-    dEa -= (fra - fla) * ci;
+    dEa = div32(dEa, fra, fla, ch, co);
     const float frb = flux_fp32(vr.y, cr, Em1.y, e0.y, Ep1.y, Ep2.y);
     const float flb = flux_fp32(vl.y, cl, Em2.y, Em1.y, e0.y, Ep1.y);
-    dEb -= (frb - flb) * ci;
+    dEb = div32(dEb, frb, flb, ch, co);
   }
   const float2 lam = ld2(sP + L.v(g, 10) + q);
   const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
   if (w.active && D.z0 + g < d.n[2])
     st2_stream(A.Enew + D.p0 + (long long)g * d.s[2] + q,
-               make_float2(e0.x + w.dt * (dEa - mfa), e0.y + w.dt * (dEb - mfb)));
+               make_float2(upd32(e0.x, dEa, mfa, w.dthi, w.dtlo), upd32(e0.y, dEb, mfb, w.dthi, w.dtlo)));
 }
 
 // one field (mem == nullptr: A, S, nitems) or the members of an ensemble

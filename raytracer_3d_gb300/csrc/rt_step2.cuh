@@ -50,7 +50,8 @@ template <> __device__ __forceinline__ float face_flux<float>(const StepArgs<flo
   return flux_fp32(v, A.t32.hcfl[a][pidx(F)], Ea, Eb, Ec, Ed);
 }
 
-// dE -= (fr - fl) / d(F)
+// binary64: dE -= (fr - fl) / d(F); binary32: acc += (fl - fr) * dt/d(F)
+// (div32, the two-term constant)
 template <class T> __device__ __forceinline__ T div_acc(const StepArgs<T>& A, int a, int F, T dE,
                                                         T fr, T fl);
 template <> __device__ __forceinline__ double div_acc<double>(const StepArgs<double>& A, int a,
@@ -60,7 +61,7 @@ template <> __device__ __forceinline__ double div_acc<double>(const StepArgs<dou
 }
 template <> __device__ __forceinline__ float div_acc<float>(const StepArgs<float>& A, int a, int F,
                                                            float dE, float fr, float fl) {
-  return dE - (fr - fl) * A.t32.inv_d[a][pidx(F)];
+  return div32(dE, fr, fl, A.t32.chi[a][pidx(F)], A.t32.clo[a][pidx(F)]);
 }
 
 // Band schedule of the plane items.  sweep = 0: for band of `band` m
@@ -166,8 +167,7 @@ __device__ __forceinline__ void plane_item(const StepArgs<T>& A, const PlaneSche
       if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p)));
       st_stream(A.Enew + p, dadd(e0, dmul(A.dt, dsub(dE, mf))));
     } else {
-      const T mf = e0 * ld_stream(A.lam[0] + p);
-      st_stream(A.Enew + p, (T)(e0 + (T)A.dt * (dE - mf)));
+      st_stream(A.Enew + p, upd32(e0, dE, e0 * ld_stream(A.lam[0] + p), A.dthi, A.dtlo));
     }
   }
   __syncthreads();  // shared memory is reused by the next item

@@ -87,7 +87,7 @@ __host__ __device__ __forceinline__ bool tma_ok(const Dims& d) {
 template <class T>
 struct ItemDesc {
   long long vloff[6];     // offset of the left-face velocities of (x,y)=(0,0), axes 2..5
-  T kcfl_r[6], kinv_r[6], kcfl_l[6];   // binary32 grid constants of the two faces
+  T kcfl_r[6], kch_r[6], kcl_r[6], kcfl_l[6];   // binary32 grid constants of the two faces
   double d_r[6], d_l[6];               // binary64 grid spacings of the two faces
 };
 // shared-memory bytes of the descriptor, rounded to the 16-byte alignment of
@@ -119,14 +119,15 @@ __device__ __forceinline__ long long nb_plane(const Dims& d, const int c[6], int
   return p;
 }
 
-// grid constants of one face: binary32 form keeps dt/(2d) and 1/d, binary64
-// keeps d (the reference divides)
+// grid constants of one face: binary32 form keeps dt/(2d) and dt/d (as
+// chi + clo), binary64 keeps d (the reference divides)
 template <class T> struct FaceK;
 template <> struct FaceK<float> {
-  float cfl, inv;
-  __device__ __forceinline__ void load(const StepArgs<float>& A, int a, int F, bool with_inv) {
+  float cfl, chi, clo;
+  __device__ __forceinline__ void load(const StepArgs<float>& A, int a, int F, bool with_div) {
     cfl = A.t32.hcfl[a][pidx(F)];
-    inv = with_inv ? A.t32.inv_d[a][pidx(F)] : 0.f;
+    chi = with_div ? A.t32.chi[a][pidx(F)] : 0.f;
+    clo = with_div ? A.t32.clo[a][pidx(F)] : 0.f;
   }
 };
 template <> struct FaceK<double> {
@@ -151,9 +152,10 @@ __device__ __forceinline__ T ucfl_at(const T* base, long long i) {
   if constexpr (sizeof(T) == 8) return base[i];
   else return T(0);
 }
-// dE -= (fr - fl)/d with the right face's constants
+// binary64: dE -= (fr - fl)/d; binary32: acc += (fl - fr)*dt/d (div32),
+// with the right face's constants
 __device__ __forceinline__ float kdiv(const FaceK<float>& kr, float dE, float fr, float fl) {
-  return dE - (fr - fl) * kr.inv;
+  return div32(dE, fr, fl, kr.chi, kr.clo);
 }
 __device__ __forceinline__ double kdiv(const FaceK<double>& kr, double dE, double fr, double fl) {
   return dsub(dE, ddiv(dsub(fr, fl), kr.d));
@@ -228,7 +230,8 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
       if (d.n[a] > 1) {
         if constexpr (sizeof(T) == 4) {
           desc->kcfl_r[a] = A.t32.hcfl[a][pidx(c[a] + 1)];
-          desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
+          desc->kch_r[a] = A.t32.chi[a][pidx(c[a] + 1)];
+          desc->kcl_r[a] = A.t32.clo[a][pidx(c[a] + 1)];
           desc->kcfl_l[a] = A.t32.hcfl[a][pidx(c[a])];
         } else {
           desc->d_r[a] = A.g.d[a][pidx(c[a] + 1)];
@@ -245,9 +248,11 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
     vloff[a] = desc->vloff[a];
     if constexpr (sizeof(T) == 4) {
       kr[a].cfl = desc->kcfl_r[a];
-      kr[a].inv = desc->kinv_r[a];
+      kr[a].chi = desc->kch_r[a];
+      kr[a].clo = desc->kcl_r[a];
       kl[a].cfl = desc->kcfl_l[a];
-      kl[a].inv = 0.f;
+      kl[a].chi = 0.f;
+      kl[a].clo = 0.f;
     } else {
       kr[a].d = desc->d_r[a];
       kl[a].d = desc->d_l[a];
@@ -335,8 +340,7 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
         if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p0 + q)));
         st_stream(A.Enew + p0 + q, dadd(e0, dmul(A.dt, dsub(dE, mf))));
       } else {
-        const T mf = e0 * ld_stream(A.lam[0] + p0 + q);
-        st_stream(A.Enew + p0 + q, (T)(e0 + (T)A.dt * (dE - mf)));
+        st_stream(A.Enew + p0 + q, upd32(e0, dE, e0 * ld_stream(A.lam[0] + p0 + q), A.dthi, A.dtlo));
       }
     }
   }

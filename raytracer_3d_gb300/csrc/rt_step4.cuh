@@ -22,7 +22,7 @@ template <class T>
 struct GroupDesc {
   long long vloff[6];      // axes 3..5: left-face velocity offset of (0,0,z0)
   long long zvoff[2];      // z face 0 of the group: offset into vel[2] (or vlo[2] when z0 == 0)
-  T kcfl_r[6], kinv_r[6], kcfl_l[6];
+  T kcfl_r[6], kch_r[6], kcl_r[6], kcfl_l[6];
   double d_r[6], d_l[6];
 };
 
@@ -135,7 +135,8 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
       if (d.n[a] > 1) {
         if constexpr (sizeof(T) == 4) {
           desc->kcfl_r[a] = A.t32.hcfl[a][pidx(c[a] + 1)];
-          desc->kinv_r[a] = A.t32.inv_d[a][pidx(c[a] + 1)];
+          desc->kch_r[a] = A.t32.chi[a][pidx(c[a] + 1)];
+          desc->kcl_r[a] = A.t32.clo[a][pidx(c[a] + 1)];
           desc->kcfl_l[a] = A.t32.hcfl[a][pidx(c[a])];
         } else {
           desc->d_r[a] = A.g.d[a][pidx(c[a] + 1)];
@@ -162,9 +163,11 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
     vloff[a] = desc->vloff[a];
     if constexpr (sizeof(T) == 4) {
       kr[a].cfl = desc->kcfl_r[a];
-      kr[a].inv = desc->kinv_r[a];
+      kr[a].chi = desc->kch_r[a];
+      kr[a].clo = desc->kcl_r[a];
       kl[a].cfl = desc->kcfl_l[a];
-      kl[a].inv = 0.f;
+      kl[a].chi = 0.f;
+      kl[a].clo = 0.f;
     } else {
       kr[a].d = desc->d_r[a];
       kl[a].d = desc->d_l[a];
@@ -281,8 +284,7 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
       if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + pc)));
       st_stream(A.Enew + pc, dadd(e0, dmul(A.dt, dsub(dE, mf))));
     } else {
-      const T mf = e0 * ld_stream(A.lam[0] + pc);
-      st_stream(A.Enew + pc, (T)(e0 + (T)A.dt * (dE - mf)));
+      st_stream(A.Enew + pc, upd32(e0, dE, e0 * ld_stream(A.lam[0] + pc), A.dthi, A.dtlo));
     }
   }
   __syncthreads();

@@ -34,7 +34,7 @@ struct WsDesc {
   const float* vl[4];      // left-face velocities at (0,0), axes z..m
   const float* b0x;        // face-0 x velocities of the plane (index y)
   const float* b0y;        // face-0 y velocities of the plane (index x)
-  float kcfl_r[4], kinv_r[4], kcfl_l[4];
+  float kcfl_r[4], kch_r[4], kcl_r[4], kcfl_l[4];   // dt/(2d) right, dt/d = kch + kcl, dt/(2d) left
   int member;              // batched form: index of the member the item belongs to
 };
 
@@ -172,7 +172,7 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
     const long long p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
                          (long long)c[5] * d.s[5];
     const float* vlp = nullptr;
-    float kr = 0.f, ki = 0.f, kl = 0.f;
+    float kr = 0.f, kh = 0.f, ko = 0.f, kl = 0.f;
     if (lane >= 2 && lane < 6) {
       const int a = lane;
       if (c[a] > 0) {
@@ -185,7 +185,8 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
       }
       if (d.n[a] > 1) {
         kr = A.t32.hcfl[a][pidx(c[a] + 1)];
-        ki = A.t32.inv_d[a][pidx(c[a] + 1)];
+        kh = A.t32.chi[a][pidx(c[a] + 1)];
+        ko = A.t32.clo[a][pidx(c[a] + 1)];
         kl = A.t32.hcfl[a][pidx(c[a])];
       }
     }
@@ -217,7 +218,8 @@ __device__ __forceinline__ void ws_produce(const StepArgs<float>& A, const Plane
     if (lane >= 2 && lane < 6) {
       D.vl[lane - 2] = vlp;
       D.kcfl_r[lane - 2] = kr;
-      D.kinv_r[lane - 2] = ki;
+      D.kch_r[lane - 2] = kh;
+      D.kcl_r[lane - 2] = ko;
       D.kcfl_l[lane - 2] = kl;
     }
     if (lane == 0) {

@@ -102,13 +102,15 @@ __global__ void __launch_bounds__(NT + 32, 1)
   const int xm = x0 > 0 ? x0 - 1 : 0, xmm = x0 > 1 ? x0 - 2 : 0;
   const bool has_right = x0 + 2 < nx;
   const float cxa = A.t32.hcfl[0][pidx(x0 + 1)], cxb = A.t32.hcfl[0][pidx(x0 + 2)];
-  const float ixa = A.t32.inv_d[0][pidx(x0 + 1)], ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  const float hxa = A.t32.chi[0][pidx(x0 + 1)], hxb = A.t32.chi[0][pidx(x0 + 2)];
+  const float oxa = A.t32.clo[0][pidx(x0 + 1)], oxb = A.t32.clo[0][pidx(x0 + 2)];
   const float cxl = A.t32.hcfl[0][pidx(x0)];
-  float cy[R], iy[R];
+  float cy[R], hy[R], oy[R];
 #pragma unroll
   for (int r = 0; r < R; r++) {
     cy[r] = A.t32.hcfl[1][pidx(yrow[r] + 1)];
-    iy[r] = A.t32.inv_d[1][pidx(yrow[r] + 1)];
+    hy[r] = A.t32.chi[1][pidx(yrow[r] + 1)];
+    oy[r] = A.t32.clo[1][pidx(yrow[r] + 1)];
   }
   const float cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
   int ecol[R + 4];   // rows y0-2 .. y0+R+1 (clamped), column pair x0
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
     yy = yy < 0 ? 0 : (yy > ny - 1 ? ny - 1 : yy);
     ecol[j] = yy * nx + x0;
   }
-  const float dt = (float)A.dt;
+  const float dthi = A.dthi, dtlo = A.dtlo;
 
   W2Regs<R> cur;
   int s = 0;
@@ -133,11 +135,12 @@ __global__ void __launch_bounds__(NT + 32, 1)
     w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur, wk.z > 0);
     const WsDesc& D = desc[s];
     const long long p0 = D.p0;
-    float kcr[4], kir[4], kcl[4];
+    float kcr[4], khr[4], kor[4], kcl[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       kcr[a] = D.kcfl_r[a];
-      kir[a] = D.kinv_r[a];
+      khr[a] = D.kch_r[a];
+      kor[a] = D.kcl_r[a];
       kcl[a] = D.kcfl_l[a];
     }
     if (!ws_wait(&full[s], par, A.status)) return;
@@ -188,11 +191,10 @@ __global__ void __launch_bounds__(NT + 32, 1)
     for (int r = 0; r < R; r++) {
       const float2 e0 = ec[r + 2];
       const int q = yrow[r] * nx + x0;
-      float dEa = 0.f, dEb = 0.f;
-      dEa -= (fxa[r] - fxl[r]) * ixa;
-      dEb -= (fxb[r] - fxa[r]) * ixb;
-      dEa -= (fy[r + 1].x - fy[r].x) * iy[r];
-      dEb -= (fy[r + 1].y - fy[r].y) * iy[r];
+      float dEa = div32(0.f, fxa[r], fxl[r], hxa, oxa);
+      float dEb = div32(0.f, fxb[r], fxa[r], hxb, oxb);
+      dEa = div32(dEa, fy[r + 1].x, fy[r].x, hy[r], oy[r]);
+      dEb = div32(dEb, fy[r + 1].y, fy[r].y, hy[r], oy[r]);
 #pragma unroll
       for (int a = 2; a < 6; a++) {
         if (d.n[a] <= 1) continue;
@@ -211,11 +213,12 @@ __global__ void __launch_bounds__(NT + 32, 1)
           flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
         }
         if (a == 2) zcarry[r] = make_float2(fra, frb);
-        dEa -= (fra - fla) * kir[a - 2];
-        dEb -= (frb - flb) * kir[a - 2];
+        dEa = div32(dEa, fra, fla, khr[a - 2], kor[a - 2]);
+        dEb = div32(dEb, frb, flb, khr[a - 2], kor[a - 2]);
       }
       const float mfa = e0.x * cur.lam[r].x, mfb = e0.y * cur.lam[r].y;
-      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, make_float2(e0.x + dt * (dEa - mfa), e0.y + dt * (dEb - mfb)));
+      if (y0 + r < ny)
+        st2_stream(A.Enew + p0 + q, make_float2(upd32(e0.x, dEa, mfa, dthi, dtlo), upd32(e0.y, dEb, mfb, dthi, dtlo)));
     }
     mbar_arrive(&empty[s]);
     s = sn;

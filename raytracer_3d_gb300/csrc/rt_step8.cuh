@@ -102,7 +102,7 @@ struct W3Prep {
   const float* src;   // null: no copy on this lane
   float* dst;
   uint32_t bytes;
-  float kr, ki, kl;   // lanes 2..5: constants of axis `lane`
+  float kr, kh, ko, kl;   // lanes 2..5: constants of axis `lane`
 };
 __device__ __forceinline__ W3Prep w3_prepare(const StepArgs<float>& A, const PlaneSched& S, long long li,
                                              float* sP) {
@@ -114,10 +114,11 @@ __device__ __forceinline__ W3Prep w3_prepare(const StepArgs<float>& A, const Pla
   P.p0 = (long long)c[2] * d.s[2] + (long long)c[3] * d.s[3] + (long long)c[4] * d.s[4] +
          (long long)c[5] * d.s[5];
   const long long p0 = P.p0;
-  P.kr = P.ki = P.kl = 0.f;
+  P.kr = P.kh = P.ko = P.kl = 0.f;
   if (lane >= 2 && lane < 6 && d.n[lane] > 1) {
     P.kr = A.t32.hcfl[lane][pidx(c[lane] + 1)];
-    P.ki = A.t32.inv_d[lane][pidx(c[lane] + 1)];
+    P.kh = A.t32.chi[lane][pidx(c[lane] + 1)];
+    P.ko = A.t32.clo[lane][pidx(c[lane] + 1)];
     P.kl = A.t32.hcfl[lane][pidx(c[lane])];
   }
   const int nx = d.n[0], ny = d.n[1];
@@ -171,7 +172,8 @@ __device__ __forceinline__ void w3_commit(const W3Prep& P, const Dims& d, int me
   const int lane = threadIdx.x & 31;
   if (lane >= 2 && lane < 6) {
     D->kcfl_r[lane - 2] = P.kr;
-    D->kinv_r[lane - 2] = P.ki;
+    D->kch_r[lane - 2] = P.kh;
+    D->kcl_r[lane - 2] = P.ko;
     D->kcfl_l[lane - 2] = P.kl;
   }
   if (lane == 0) {
@@ -208,8 +210,8 @@ struct W3Geom {
   int nx, ny, nxy, x0, y0, xm, xmm, yb_off;
   bool has_right;
   int yrow[R], ecol[R + 4];
-  float cxa, cxb, ixa, ixb, cxl, cyb, dt;
-  float cy[R], iy[R];
+  float cxa, cxb, hxa, hxb, oxa, oxb, cxl, cyb, dthi, dtlo;
+  float cy[R], hy[R], oy[R];
 };
 
 template <int R>
@@ -229,13 +231,16 @@ __device__ __forceinline__ void w3_geom(const StepArgs<float>& A, int t, W3Geom<
   g.has_right = x0 + 2 < nx;
   g.cxa = A.t32.hcfl[0][pidx(x0 + 1)];
   g.cxb = A.t32.hcfl[0][pidx(x0 + 2)];
-  g.ixa = A.t32.inv_d[0][pidx(x0 + 1)];
-  g.ixb = A.t32.inv_d[0][pidx(x0 + 2)];
+  g.hxa = A.t32.chi[0][pidx(x0 + 1)];
+  g.hxb = A.t32.chi[0][pidx(x0 + 2)];
+  g.oxa = A.t32.clo[0][pidx(x0 + 1)];
+  g.oxb = A.t32.clo[0][pidx(x0 + 2)];
   g.cxl = A.t32.hcfl[0][pidx(x0)];
 #pragma unroll
   for (int r = 0; r < R; r++) {
     g.cy[r] = A.t32.hcfl[1][pidx(g.yrow[r] + 1)];
-    g.iy[r] = A.t32.inv_d[1][pidx(g.yrow[r] + 1)];
+    g.hy[r] = A.t32.chi[1][pidx(g.yrow[r] + 1)];
+    g.oy[r] = A.t32.clo[1][pidx(g.yrow[r] + 1)];
   }
   g.cyb = A.t32.hcfl[1][pidx(y0 < ny ? y0 : ny - 1)];
 #pragma unroll
@@ -248,7 +253,8 @@ __device__ __forceinline__ void w3_geom(const StepArgs<float>& A, int t, W3Geom<
   // face-0 y row (y0 == 0)
   g.yb_off = y0 == 0 ? RT_W3_NPL * g.nxy + ny + x0
                      : RT_W3_VY * g.nxy + ((y0 - 1 < ny - 1 ? y0 - 1 : ny - 1)) * nx + x0;
-  g.dt = (float)A.dt;
+  g.dthi = A.dthi;
+  g.dtlo = A.dtlo;
 }
 
 // one item of one consumer thread from a filled stage
@@ -258,11 +264,12 @@ __device__ __forceinline__ void w3_item(const StepArgs<float>& A, const W3Geom<R
   const Dims& d = A.d;
   const int nx = g.nx, ny = g.ny, nxy = g.nxy, x0 = g.x0, y0 = g.y0;
   const long long p0 = D.p0;
-  float kcr[4], kir[4], kcl[4];
+  float kcr[4], khr[4], kor[4], kcl[4];
 #pragma unroll
   for (int a = 0; a < 4; a++) {
     kcr[a] = D.kcfl_r[a];
-    kir[a] = D.kinv_r[a];
+    khr[a] = D.kch_r[a];
+    kor[a] = D.kcl_r[a];
     kcl[a] = D.kcfl_l[a];
   }
   float2 ec[R + 4];
@@ -316,11 +323,10 @@ __device__ __forceinline__ void w3_item(const StepArgs<float>& A, const W3Geom<R
   for (int r = 0; r < R; r++) {
     const float2 e0 = ec[r + 2];
     const int q = g.yrow[r] * nx + x0;
-    float dEa = 0.f, dEb = 0.f;
-    dEa -= (fxa[r] - fxl[r]) * g.ixa;
-    dEb -= (fxb[r] - fxa[r]) * g.ixb;
-    dEa -= (fy[r + 1].x - fy[r].x) * g.iy[r];
-    dEb -= (fy[r + 1].y - fy[r].y) * g.iy[r];
+    float dEa = div32(0.f, fxa[r], fxl[r], g.hxa, g.oxa);
+    float dEb = div32(0.f, fxb[r], fxa[r], g.hxb, g.oxb);
+    dEa = div32(dEa, fy[r + 1].x, fy[r].x, g.hy[r], g.oy[r]);
+    dEb = div32(dEb, fy[r + 1].y, fy[r].y, g.hy[r], g.oy[r]);
 #pragma unroll
     for (int a = 2; a < 6; a++) {
       if (d.n[a] <= 1) continue;
@@ -329,15 +335,16 @@ __device__ __forceinline__ void w3_item(const StepArgs<float>& A, const W3Geom<R
       const float2 vr = ld2(sE + (RT_W3_VR + a - 2) * nxy + q), vl = ld2(sE + (RT_W3_VL + a - 2) * nxy + q);
       const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
       const float fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
-      dEa -= (fra - fla) * kir[a - 2];
+      dEa = div32(dEa, fra, fla, khr[a - 2], kor[a - 2]);
       const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
       const float flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
-      dEb -= (frb - flb) * kir[a - 2];
+      dEb = div32(dEb, frb, flb, khr[a - 2], kor[a - 2]);
     }
     const float2 lam = ld2(sE + RT_W3_LAM * nxy + q);
     const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
     if (y0 + r < ny)
-      st2_stream(A.Enew + p0 + q, make_float2(e0.x + g.dt * (dEa - mfa), e0.y + g.dt * (dEb - mfb)));
+      st2_stream(A.Enew + p0 + q,
+                 make_float2(upd32(e0.x, dEa, mfa, g.dthi, g.dtlo), upd32(e0.y, dEb, mfb, g.dthi, g.dtlo)));
   }
 }
 

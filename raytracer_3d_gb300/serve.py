@@ -343,9 +343,20 @@ class GpuExecutor:
 
 
 class SequentialExecutor(GpuExecutor):
-    """Baseline: one request at a time, each stepped alone (rt_integrate)."""
+    """Baseline: one request at a time, each stepped alone (rt_integrate),
+    with the given step schedule (e.g. ("fast", 8, 256, 0) for binary64)."""
 
     overlap_setup = False  # set-up inline: no overlap in the baseline
+
+    def __init__(self, precision="fp64", schedule=None):
+        super().__init__(precision)
+        self.schedule = schedule
+
+    def admit(self, r):
+        m = super().admit(r)
+        if self.schedule:
+            m.set_tuning(*self.schedule)
+        return m
 
     def step(self, members, n):
         for m in members:

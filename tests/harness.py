@@ -56,3 +56,38 @@ def max_rel(a, b):
     den = float(np.max(np.abs(b)))
     num = float(np.max(np.abs(a - b)))
     return num / den if den > 0 else num
+
+
+def vol_weights(model):
+    """the six 1D cell widths of a model's interior (binary64)"""
+    return [model.grid["xyzklm"[a]]["dt"][ONX:ONX + model.n[a]] for a in range(6)]
+
+
+def energy_sum(E, widths):
+    """total energy sum(E * vol) of an interior 6D array, vol the product of
+    the cell widths, accumulated one m plane at a time (no full-size
+    temporaries at 32^6)"""
+    v5 = np.ones([len(w) for w in widths[:5]])
+    for a in range(5):
+        shp = [1] * 5
+        shp[a] = len(widths[a])
+        v5 = v5 * widths[a].reshape(shp)
+    tot = 0.0
+    for m in range(E.shape[5]):
+        tot += float(np.sum(np.asarray(E[..., m], dtype=np.float64) * v5)) * float(widths[5][m])
+    return tot
+
+
+def error_norms(got, ref):
+    """relative L2 and L-infinity (relative to max |ref|) of got - ref,
+    accumulated one m plane at a time"""
+    num2 = den2 = 0.0
+    dmax = rmax = 0.0
+    for m in range(ref.shape[5]):
+        r = np.asarray(ref[..., m], dtype=np.float64)
+        d = np.asarray(got[..., m], dtype=np.float64) - r
+        num2 += float(np.sum(d * d))
+        den2 += float(np.sum(r * r))
+        dmax = max(dmax, float(np.max(np.abs(d))))
+        rmax = max(rmax, float(np.max(np.abs(r))))
+    return (num2 ** 0.5) / (den2 ** 0.5), dmax / rmax

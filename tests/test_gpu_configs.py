@@ -1,0 +1,117 @@
+"""The workloads at their full sizes and lengths.
+
+* 32^6 plain binary64 (the bench workload): one step of each bit-exact
+  schedule from the same state gives the same field bit for bit, and the
+  fast schedule is within 1e-12 relative L-infinity of them.
+* 32^6 binary32, 1000 steps, against binary64 (the fast schedule, itself
+  held to 1e-12 per step of the reference's arithmetic): relative L2
+  <= 1e-5 and relative total-energy drift <= 1e-9.
+* the 48-member binary32 ensemble, 500 steps in one batch, against every
+  member run alone in binary64: the same bounds per member.
+
+These runs hold up to about 210 GB of device memory and take minutes; each
+binary64 handle is closed before the binary32 one is built."""
+import numpy as np
+import pytest
+
+from harness import configs, energy_sum, error_norms, max_rel, vol_weights
+
+pytestmark = pytest.mark.gpu
+
+FP64_STEP_TOL = 1e-12
+FP32_L2_TOL = 1e-5        # relative L2 of E against binary64
+FP32_DRIFT_TOL = 1e-9     # relative total-energy difference against binary64
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    import __graft_entry__ as g
+    g.build()
+
+
+def test_config2_schedules_agree_at_32():
+    exp = configs.jet_large()
+    m = configs.build_model(exp, "fp64", padded=False)
+    try:
+        E0 = m.E.copy(order="F")
+        out = {}
+        for sched in ("tma", "split", "fast"):
+            m.E = E0
+            m.set_state()
+            m.set_tuning(sched, 8, 256)
+            m.integrate(1)
+            out[sched] = m.get_state()
+        assert np.array_equal(out["tma"], out["split"])
+        rel = max_rel(out["fast"], out["split"])
+        print("32^6 binary64: tma == split bit for bit; fast within %.2e" % rel)
+        assert rel <= FP64_STEP_TOL
+    finally:
+        m.close()
+
+
+def test_config3_fp32_1000_steps_at_32():
+    exp = configs.jet_large()
+    steps = 1000
+    m64 = configs.build_model(exp, "fp64", padded=False)
+    try:
+        w = vol_weights(m64)
+        e_start = energy_sum(m64.E, w)
+        m64.set_tuning("fast", 8, 256)
+        m64.integrate(steps)
+        ref = m64.get_state()
+    finally:
+        m64.close()
+    m32 = configs.build_model(exp, "fp32", padded=False)
+    try:
+        m32.set_tuning("w2z", 8, 512, 1)
+        m32.integrate(steps)
+        got = m32.get_state()
+    finally:
+        m32.close()
+    assert np.isfinite(got).all()
+    l2, linf = error_norms(got, ref)
+    e64, e32 = energy_sum(ref, w), energy_sum(got, w)
+    drift = abs(e32 - e64) / abs(e64)
+    print("jet_large 32^6, %d steps, binary32 against binary64: L2 %.3e  Linf %.3e  energy %.3e  "
+          "(binary64 energy change over the run %.3e)" % (steps, l2, linf, drift, abs(e64 - e_start) / abs(e_start)))
+    assert l2 <= FP32_L2_TOL
+    assert drift <= FP32_DRIFT_TOL
+
+
+def test_config4_ensemble_500_steps_against_fp64():
+    from raytracer_3d_gb300.batch import Batch
+    rng = np.random.default_rng(2024)
+    exps = [configs.ensemble_member(rng, steps=500) for _ in range(48)]
+    steps = 500
+    models = [configs.build_model(e, "fp32", padded=False) for e in exps]
+    b = Batch(models)
+    try:
+        b.set_tuning(8, 512, 1, 16)
+        b.set_persistent(512)
+        b.integrate(steps)
+        b.sync()
+        got = [m.get_state() for m in models]
+        weights = [vol_weights(m) for m in models]
+    finally:
+        b.close()
+        for m in models:
+            m.close()
+    worst = {"l2": 0.0, "linf": 0.0, "drift": 0.0}
+    for e, g, w in zip(exps, got, weights):
+        m = configs.build_model(e, "fp64", padded=False)
+        try:
+            m.set_tuning("fast", 8, 256)
+            m.integrate(steps)
+            ref = m.get_state()
+        finally:
+            m.close()
+        l2, linf = error_norms(g, ref)
+        e64, e32 = energy_sum(ref, w), energy_sum(g, w)
+        drift = abs(e32 - e64) / abs(e64)
+        worst["l2"] = max(worst["l2"], l2)
+        worst["linf"] = max(worst["linf"], linf)
+        worst["drift"] = max(worst["drift"], drift)
+    print("48-member ensemble, %d steps, binary32 batch against binary64 alone (worst member): "
+          "L2 %.3e  Linf %.3e  energy %.3e" % (steps, worst["l2"], worst["linf"], worst["drift"]))
+    assert worst["l2"] <= FP32_L2_TOL
+    assert worst["drift"] <= FP32_DRIFT_TOL

@@ -46,9 +46,9 @@ def test_fp32_jet_1000_steps_against_fp64():
         print("jet_large 16^6, 1000 steps: L2 %.3e  Linf %.3e  energy fp32 vs fp64 %.3e  "
               "(fp64 energy change over the run %.3e)" % (l2, linf, drift, abs(e64 - e0) / abs(e0)))
         assert np.isfinite(got).all()
-        assert l2 <= 1e-4
-        assert linf <= 1e-3
-        assert drift <= 1e-5
+        assert l2 <= 1e-5
+        assert linf <= 1e-4
+        assert drift <= 1e-9
     finally:
         m64.close()
         m32.close()

@@ -359,7 +359,7 @@ def test_fp32_form_against_fp64_oracle(variant):
         print("fp32 vs fp64 oracle after 200 steps: L2 %.3e Linf %.3e energy %.3e" % (l2, linf, drift))
         assert l2 <= 1e-5
         assert linf <= 1e-4
-        assert drift <= 1e-6
+        assert drift <= 1e-9
     finally:
         m.close()
 
