@@ -66,6 +66,10 @@ def _load(threads):
     lib.orc_set_forcing.restype = ctypes.c_int
     lib.orc_set_forcing.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     lib.orc_apply_forcing.argtypes = [P]
+    lib.orc_create_light.restype = P
+    lib.orc_create_light.argtypes = [ctypes.c_int] * 6
+    lib.orc_point_steps.argtypes = [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                    ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]
     _libs[name] = lib
     return lib
 
@@ -73,16 +77,18 @@ def _load(threads):
 class Oracle:
     """Module state of main_module.f90 in C memory, with numpy views."""
 
-    def __init__(self, n, threads=False):
+    def __init__(self, n, threads=False, light=False):
+        """light=True: grids, background and scalars only, for the per-cell
+        restatement (point_steps) on fields too large for the arrays"""
         self.n = tuple(int(x) for x in n)
         self.lib = _load(threads)
-        self.s = self.lib.orc_create(*self.n)
+        self.s = (self.lib.orc_create_light if light else self.lib.orc_create)(*self.n)
         if not self.s:
             raise MemoryError("oracle allocation failed")
         P6 = tuple(x + 2 * ONX for x in self.n)
         P3 = P6[:3]
         for i, name in enumerate(FIELDS6):
-            setattr(self, name, self._view(i, P6))
+            setattr(self, name, None if light else self._view(i, P6))
         for i, name in enumerate(FIELDS3):
             setattr(self, name, self._view(32 + i, P3))
         self.grid = {}
@@ -152,3 +158,19 @@ class Oracle:
 
     def threads(self):
         return self.lib.orc_threads()
+
+    def point_steps(self, E0, cells):
+        """E after one step at the given interior cells (an (K, 6) array of
+        Fortran indices i,j,k,l,n,m) from the interior pre-step state E0
+        (shape n, any order; copied to Fortran order)"""
+        E0 = np.asfortranarray(E0, dtype=np.float64)
+        assert E0.shape == self.n
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        assert cells.ndim == 2 and cells.shape[1] == 6
+        for a in range(6):
+            assert cells[:, a].min() >= 1 and cells[:, a].max() <= self.n[a]
+        out = np.empty(len(cells))
+        self.lib.orc_point_steps(self.s, E0.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                 cells.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(cells),
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out

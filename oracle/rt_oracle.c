@@ -87,6 +87,36 @@ orc_state* orc_create(int nx, int ny, int nz, int nk, int nl, int nm) {
   return s;
 }
 
+/* grids, background and scalars only (no 6D fields): the context of the
+ * per-cell restatement below, for fields too large for the whole-array
+ * oracle */
+orc_state* orc_create_light(int nx, int ny, int nz, int nk, int nl, int nm) {
+  orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
+  if (!s) return NULL;
+  int nn[6] = {nx, ny, nz, nk, nl, nm};
+  long long st = 1;
+  for (int a = 0; a < 6; a++) {
+    s->n[a] = nn[a];
+    s->P[a] = nn[a] + 2 * ONX;
+    s->S[a] = st;
+    st *= s->P[a];
+  }
+  s->len6 = st;
+  s->len3 = s->P[0] * s->P[1] * s->P[2];
+  s->sign_of_omega_i = 1.0;
+  s->f0 = 1e-4;
+  s->upper_refl = s->lower_refl = 1;
+  for (int f = 0; f < 11; f++) {
+    s->f3[f] = (double*)calloc((size_t)s->len3, sizeof(double));
+    if (!s->f3[f]) { orc_destroy(s); return NULL; }
+  }
+  for (int f = 0; f < 24; f++) {
+    s->g1[f] = (double*)calloc((size_t)s->P[f / 4], sizeof(double));
+    if (!s->g1[f]) { orc_destroy(s); return NULL; }
+  }
+  return s;
+}
+
 void orc_destroy(orc_state* s) {
   if (!s) return;
   for (int f = 0; f < ORC_N6D; f++) free(s->f6[f]);
@@ -693,4 +723,202 @@ double orc_max_rate(orc_state* s) {
     best = fmax2(best, r);
   }
   return best;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Per-cell restatement (spot checks of fields too large for the arrays      */
+/* above): the state after one step at one interior cell, from the pre-step  */
+/* interior state, the grids and the background.  Every value is formed by   */
+/* the same expressions, in the same order, as orc_calc_parameter (the       */
+/* dispersion relation, the pair averages with the overwritten aloc, the     */
+/* clamps), the boundary fill of orc_integrate and superbee_axis /           */
+/* divergence_axis / the update, so it is bit-identical to the whole-array   */
+/* oracle (checked on small cases by the tests).                             */
+/* ------------------------------------------------------------------------ */
+
+/* om_e (and om_i) at a padded point, calc_parameter.f90:13-27 */
+static double pt_om(const orc_state* s, const int x[6], double* om_i_out) {
+  const double* kt = s->g1[4 * 3 + 0];
+  const double* lt = s->g1[4 * 4 + 0];
+  const double* mt = s->g1[4 * 5 + 0];
+  const double* Nsqr = s->f3[0]; const double* U = s->f3[1]; const double* V = s->f3[2];
+  const double f0 = s->f0;
+  const int l = x[3], n = x[4], m = x[5];
+  double kh2 = lt[PO(n)] * lt[PO(n)] + kt[PO(l)] * kt[PO(l)];
+  long long q = i3(s, x[0], x[1], x[2]);
+  double oi = s->sign_of_omega_i *
+              sqrt((Nsqr[q] * kh2 + f0 * f0 * (mt[PO(m)] * mt[PO(m)])) / (mt[PO(m)] * mt[PO(m)] + kh2));
+  if (om_i_out) *om_i_out = oi;
+  return oi + kt[PO(l)] * U[q] + lt[PO(n)] * V[q];
+}
+
+/* the pair average aloc(t along b) = 0.5*(om_e(t) + om_e(t+1)) at point x */
+static double pt_avg(const orc_state* s, const int x[6], int b, int t) {
+  int y[6];
+  memcpy(y, x, sizeof y);
+  y[b] = t;
+  double e0 = pt_om(s, y, NULL);
+  y[b] = t + 1;
+  double e1 = pt_om(s, y, NULL);
+  return 0.5 * (e0 + e1);
+}
+
+/* face velocity of axis a at face index f (Fortran), the other indices
+ * those of `cell` (interior) */
+static double pt_vel(const orc_state* s, int a, const int cell[6], int f) {
+  int x[6];
+  memcpy(x, cell, sizeof x);
+  x[a] = f;
+  const double f0 = s->f0;
+  if (a == 0 || a == 1) {                 /* xdot / ydot: difference along k / l */
+    const int b = a + 3;
+    if (s->n[a] > 1 && s->n[b] > 1) {
+      const double* d = s->g1[4 * b + 2];
+      double q = (pt_avg(s, x, b, x[b]) - pt_avg(s, x, b, x[b] - 1)) / d[PO(x[b])];
+      if (f == s->n[a]) q = fmax2(0.0, q);
+      if (f == 0) q = -fmax2(0.0, -q);
+      return q;
+    }
+    if (f < 1 || f > s->n[a]) return 0.0;   /* the analytic branch fills the interior only */
+    const double* kt = s->g1[4 * 3 + 0];
+    const double* lt = s->g1[4 * 4 + 0];
+    const double* mt = s->g1[4 * 5 + 0];
+    const double* Nsqr = s->f3[0];
+    const double* UV = a == 0 ? s->f3[1] : s->f3[2];
+    double oi;
+    pt_om(s, x, &oi);
+    double kh2 = lt[PO(x[4])] * lt[PO(x[4])] + kt[PO(x[3])] * kt[PO(x[3])];
+    long long q = i3(s, x[0], x[1], x[2]);
+    double m2 = mt[PO(x[5])] * mt[PO(x[5])];
+    double den = m2 + kh2;
+    return UV[q] + (Nsqr[q] - f0 * f0) / oi * m2 / (den * den) * (a == 0 ? kt[PO(x[3])] : lt[PO(x[4])]);
+  }
+  if (a == 3 || a == 4) {                 /* kdot / ldot: difference along x / y */
+    const int b = a - 3;
+    if (!(s->n[b] > 1 && s->n[a] > 1)) return 0.0;
+    const double* d = s->g1[4 * b + 2];
+    int xm[6];
+    memcpy(xm, x, sizeof xm);
+    xm[b] = x[b] - 1;
+    double q = (pt_avg(s, x, a, f) - pt_avg(s, xm, a, f)) / d[PO(x[b])];
+    double v = -q;
+    if (f == s->n[a]) v = fmax2(0.0, v);
+    if (f == 0) v = -fmax2(0.0, -v);
+    return v;
+  }
+  if (a == 2) {                           /* zdot: difference along m, no analytic branch */
+    const double* d = s->g1[4 * 5 + 2];
+    double q = (pt_avg(s, x, 5, x[5]) - pt_avg(s, x, 5, x[5] - 1)) / d[PO(x[5])];
+    if (f == s->n[2] && !s->upper_refl) q = fmax2(0.0, q);
+    if (f == 0 && !s->lower_refl) q = -fmax2(0.0, -q);
+    return q;
+  }
+  {                                       /* mdot: difference along z */
+    const double* d = s->g1[4 * 2 + 2];
+    int xm[6];
+    memcpy(xm, x, sizeof xm);
+    xm[2] = x[2] - 1;
+    double q = (pt_avg(s, x, 5, f) - pt_avg(s, xm, 5, f)) / d[PO(x[2])];
+    double v = -q;
+    if (f == s->n[5]) v = fmax2(0.0, v);
+    if (f == 0) v = -fmax2(0.0, -v);
+    return v;
+  }
+}
+
+/* E at `cell` with index t along axis a after the boundary fill of
+ * orc_integrate (reflection with m reversed, else the edge cell); E0 is
+ * the interior, x fastest */
+static double pt_E(const orc_state* s, const double* E0, const int cell[6], int a, int t) {
+  int x[6];
+  memcpy(x, cell, sizeof x);
+  const int n = s->n[a];
+  if (t >= 1 && t <= n) {
+    x[a] = t;
+  } else if (a == 2 && t > n && s->upper_refl) {
+    x[2] = 2 * n + 1 - t;
+    x[5] = s->n[5] + 1 - x[5];
+  } else if (a == 2 && t < 1 && s->lower_refl) {
+    x[2] = 1 - t;
+    x[5] = s->n[5] + 1 - x[5];
+  } else {
+    x[a] = t < 1 ? 1 : n;
+  }
+  long long p = 0;
+  for (int b = 5; b >= 0; b--) p = p * s->n[b] + (x[b] - 1);
+  return E0[p];
+}
+
+/* superbee flux at face f of axis a (superbee_fluxes.f90:19-30) */
+static double pt_flux(const orc_state* s, const double* E0, const int cell[6], int a, int f) {
+  const double* dgrid = s->g1[4 * a + 2];
+  const double dt = s->dt;
+  double v = pt_vel(s, a, cell, f);
+  double uCFL = fabs(v * dt / dgrid[PO(f)]);
+  double Ep2 = pt_E(s, E0, cell, a, f + 2), Ep1 = pt_E(s, E0, cell, a, f + 1);
+  double Ef = pt_E(s, E0, cell, a, f), Em1 = pt_E(s, E0, cell, a, f - 1);
+  double Rjp = Ep2 - Ep1;
+  double Rj = Ep1 - Ef;
+  double Rjm = Ef - Em1;
+  double Cr;
+  if (Rj != 0.) {
+    if (v > 0) Cr = Rjm / Rj; else Cr = Rjp / Rj;
+  } else {
+    if (v > 0) Cr = Rjm * LIT_1E20; else Cr = Rjp * LIT_1E20;
+  }
+  Cr = limiter(Cr);
+  return v * (Ep1 + Ef) * 0.5 - fabs(v) * ((1. - Cr) + uCFL * Cr) * Rj * 0.5;
+}
+
+/* growth rates at an interior cell, calc_parameter.f90:240-260 */
+static void pt_lambda(const orc_state* s, const int c[6], double lam[3]) {
+  const double* kt = s->g1[4 * 3 + 0];
+  const double* lt = s->g1[4 * 4 + 0];
+  const double* dxt = s->g1[4 * 0 + 2]; const double* dyt = s->g1[4 * 1 + 2];
+  const double* dzt = s->g1[4 * 2 + 2];
+  const double* U = s->f3[1]; const double* V = s->f3[2];
+  const int i = c[0], j = c[1], k = c[2], l = c[3], n = c[4];
+  double oi;
+  pt_om(s, c, &oi);
+  long long q = i3(s, i, j, k);
+  double xd = pt_vel(s, 0, c, i), yd = pt_vel(s, 1, c, j), zd = pt_vel(s, 2, c, k);
+  lam[0] = 1. / oi * kt[PO(l)] *
+           ((xd - U[q]) * (U[i3(s, i + 1, j, k)] - U[i3(s, i - 1, j, k)]) / (2 * dxt[PO(i)]) +
+            (yd - V[q]) * (V[i3(s, i + 1, j, k)] - V[i3(s, i - 1, j, k)]) / (2 * dxt[PO(i)]));
+  lam[1] = 1. / oi * lt[PO(n)] *
+           ((xd - U[q]) * (U[i3(s, i, j + 1, k)] - U[i3(s, i, j - 1, k)]) / (2 * dyt[PO(j)]) +
+            (yd - V[q]) * (V[i3(s, i, j + 1, k)] - V[i3(s, i, j - 1, k)]) / (2 * dyt[PO(j)]));
+  lam[2] = 1. / oi * zd *
+           (kt[PO(l)] * (U[i3(s, i, j, k + 1)] - U[i3(s, i, j, k - 1)]) / (2 * dzt[PO(k)]) +
+            lt[PO(n)] * (V[i3(s, i, j, k + 1)] - V[i3(s, i, j, k - 1)]) / (2 * dzt[PO(k)]));
+}
+
+/* E after one step (integrate.f90:105-268) at the interior cells
+ * cells[6*q .. 6*q+5] (Fortran indices), from the interior pre-step state
+ * E0 (x fastest); needs the grids, background and scalars of s */
+void orc_point_steps(const orc_state* s, const double* E0, const int* cells, long long count, double* out) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (long long q = 0; q < count; q++) {
+    const int* c = cells + 6 * q;
+    double dE = 0.;
+    for (int a = 0; a < 6; a++) {
+      if (s->n[a] <= 1) continue;
+      const double* dgrid = s->g1[4 * a + 2];
+      const int f = c[a];
+      double fr = pt_flux(s, E0, c, a, f);
+      double fl = pt_flux(s, E0, c, a, f - 1);
+      dE = dE - (fr - fl) / dgrid[PO(f)];
+    }
+    double lam[3];
+    pt_lambda(s, c, lam);
+    const int use[3] = {s->n[0] > 1, s->n[1] > 1, s->n[2] > 1};
+    const double e = pt_E(s, E0, c, 0, c[0]);
+    double mf = 0.;
+    for (int cc = 0; cc < 3; cc++)
+      if (use[cc]) mf = mf + e * lam[cc];
+    dE = dE - mf;
+    out[q] = e + s->dt * dE;
+  }
 }

@@ -90,6 +90,17 @@ double orc_max_rate(orc_state* s);
 /* OpenMP threads used by the step (1 when built without OpenMP) */
 int orc_threads(void);
 
+/* Per-cell restatement for fields too large for the arrays above.
+ * orc_create_light allocates grids, background and scalars only (no 6D
+ * field; orc_calc_parameter / orc_integrate / orc_diagnose must not be
+ * called on it).  orc_point_steps writes to out[q] the state after one step
+ * at the interior cell cells[6q..6q+5] (Fortran indices i,j,k,l,n,m), from
+ * the interior pre-step state E0 (nx*ny*nz*nk*nl*nm doubles, x fastest),
+ * with the expressions and operation order of orc_calc_parameter and
+ * orc_integrate: bit-identical to the whole-array oracle. */
+orc_state* orc_create_light(int nx, int ny, int nz, int nk, int nl, int nm);
+void orc_point_steps(const orc_state* s, const double* E0, const int* cells, long long count, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,33 @@ def build_oracle(exp, threads=False):
     return o
 
 
+def build_point_oracle(exp, dt, threads=True):
+    """the per-cell oracle of an experiment: grids and background as in
+    build_oracle, dt given (the CFL-defined dt needs whole coefficient
+    fields; the caller passes the one the GPU uses, which the coefficient
+    parity tests pin on smaller cases)"""
+    o = Oracle(exp.n, threads=threads, light=True)
+    o.set_spacings(exp.d_interior)
+    o.set_scalars(dt, exp.f0, exp.sign_of_omega_i, exp.upper, exp.lower, exp.fixed)
+    rc = o.calc_grid()
+    assert rc == 0, "oracle calc_grid check failed (%d)" % rc
+    exp.background(o)
+    o.dt = dt
+    return o
+
+
+def sample_cells(n, count, rng):
+    """interior cells (Fortran indices), half of them on a boundary plane of
+    a random axis (first or last index) so that faces and z walls are hit"""
+    cells = np.stack([rng.integers(1, k + 1, size=count) for k in n], axis=1)
+    edge = rng.random(count) < 0.5
+    ax = rng.integers(0, 6, size=count)
+    hi = rng.random(count) < 0.5
+    for q in np.nonzero(edge)[0]:
+        cells[q, ax[q]] = n[ax[q]] if hi[q] else 1
+    return cells.astype(np.int32)
+
+
 def interior(n):
     return tuple(slice(ONX, ONX + k) for k in n)
 

@@ -14,7 +14,7 @@ binary64 handle is closed before the binary32 one is built."""
 import numpy as np
 import pytest
 
-from harness import configs, energy_sum, error_norms, max_rel, vol_weights
+from harness import build_point_oracle, configs, energy_sum, error_norms, max_rel, sample_cells, vol_weights
 
 pytestmark = pytest.mark.gpu
 
@@ -46,6 +46,41 @@ def test_config2_schedules_agree_at_32():
         print("32^6 binary64: tma == split bit for bit; fast within %.2e" % rel)
         assert rel <= FP64_STEP_TOL
     finally:
+        m.close()
+
+
+def test_config2_cells_against_the_oracle_at_32():
+    """1500 cells of one bit-exact step at 32^6 (half of them on a boundary
+    plane: open faces, z walls under reflection, the edges of the spectral
+    axes) against the oracle's per-cell restatement of the reference's
+    update, from the same pre-step state: bit-identical; the fast schedule
+    within 1e-12 of it"""
+    exp = configs.jet_large()
+    m = configs.build_model(exp, "fp64", padded=False)
+    po = None
+    try:
+        m.set_tuning("split", 8, 256)
+        m.integrate(10)          # outflow and refraction have built gradients by now
+        E0 = m.get_state()
+        m.integrate(1)
+        E1 = m.get_state()
+        po = build_point_oracle(exp, m.dt)
+        cells = sample_cells(exp.n, 1500, np.random.default_rng(99))
+        ref = po.point_steps(E0, cells)
+        idx = tuple((cells - 1).T)
+        got = E1[idx]
+        assert np.array_equal(got, ref), float(np.max(np.abs(got - ref)))
+        m.E = E0
+        m.set_state()
+        m.set_tuning("fast", 8, 256)
+        m.integrate(1)
+        fast = m.get_state()[idx]
+        rel = float(np.max(np.abs(fast - ref))) / float(np.max(np.abs(E1)))
+        print("32^6: %d cells of the split step equal the per-cell oracle; fast within %.2e" % (len(cells), rel))
+        assert rel <= FP64_STEP_TOL
+    finally:
+        if po is not None:
+            po.close()
         m.close()
 
 
