@@ -79,6 +79,7 @@ inline bool w3_ok(const Dims& d, int threads) {
 }
 
 // rt_persist_w2.cu (the caller checks w2_ok first)
-cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, cudaStream_t st);
+// packed: the cell-pair arithmetic on the f32x2 instructions (same results)
+cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool packed, cudaStream_t st);
 
 }  // namespace rt

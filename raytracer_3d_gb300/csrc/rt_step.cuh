@@ -71,6 +71,43 @@ __device__ __forceinline__ float flux_fp32(float v, float hcfl, float Ea, float 
   return fmaf(h, psi, v * Eu);
 }
 
+// ---- two cells at once: binary32 pairs on the packed f32x2 pipes --------
+// sm_100+ executes add / sub / mul / fma on a pair of binary32 values held
+// in a 64-bit register as one instruction, each lane rounded exactly as the
+// scalar instruction would round it (round to nearest even), so a pair
+// computed packed equals the two scalar results bit for bit.
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+// a*b + c, one rounding per lane
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 pk_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 pk_abs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+
 // Per-axis small tables of the binary32 form on the padded index range
 // (Fortran index f at position f+1): 1/d(f) (the budget's divergence),
 // dt/(2 d(f)) (the flux), and dt/d(f) as the unevaluated sum chi + clo of
@@ -97,6 +134,50 @@ __device__ __forceinline__ float div32(float acc, float fr, float fl, float chi,
 }
 __device__ __forceinline__ float upd32(float e0, float acc, float mf, float dthi, float dtlo) {
   return e0 + fmaf(-mf, dthi, fmaf(-mf, dtlo, acc));
+}
+
+// The same per-cell arithmetic for two cells at once (flux_fp32, div32,
+// upd32 lane by lane); PK selects the packed f32x2 instructions for the
+// additions and products, the limiter's selections and min / max stay
+// scalar.  Both settings give identical results.
+template <bool PK>
+__device__ __forceinline__ float2 flux2(float2 v, float2 hcfl, float2 Ea, float2 Eb, float2 Ec, float2 Ed) {
+  if constexpr (!PK) {
+    return make_float2(flux_fp32(v.x, hcfl.x, Ea.x, Eb.x, Ec.x, Ed.x), flux_fp32(v.y, hcfl.y, Ea.y, Eb.y, Ec.y, Ed.y));
+  } else {
+    const float2 Rjp = pk_sub(Ed, Ec), Rj = pk_sub(Ec, Eb), Rjm = pk_sub(Eb, Ea);
+    const bool px = v.x > 0.f, py = v.y > 0.f;
+    const float2 up = make_float2(px ? Rjm.x : Rjp.x, py ? Rjm.y : Rjp.y);
+    const float2 Eu = make_float2(px ? Eb.x : Ec.x, py ? Eb.y : Ec.y);
+    const unsigned sx = __float_as_uint(Rj.x) & 0x80000000u, sy = __float_as_uint(Rj.y) & 0x80000000u;
+    const float ax = fabsf(Rj.x), ay = fabsf(Rj.y);
+    const float tx = __uint_as_float(__float_as_uint(up.x) ^ sx), ty = __uint_as_float(__float_as_uint(up.y) ^ sy);
+    const float2 mn = make_float2(fminf(ax, tx), fminf(ay, ty));
+    const float2 mn2 = pk_mul(make_float2(2.f, 2.f), mn);
+    const float phx = fmaxf(0.f, fminf(mn2.x, fmaxf(ax, tx))), phy = fmaxf(0.f, fminf(mn2.y, fmaxf(ay, ty)));
+    const float2 psi = make_float2(__uint_as_float(__float_as_uint(phx) ^ sx), __uint_as_float(__float_as_uint(phy) ^ sy));
+    const float2 av = pk_abs(v);
+    const float2 h = pk_mul(av, pk_fma(pk_neg(hcfl), av, make_float2(0.5f, 0.5f)));
+    return pk_fma(h, psi, pk_mul(v, Eu));
+  }
+}
+template <bool PK>
+__device__ __forceinline__ float2 div2(float2 acc, float2 fr, float2 fl, float2 chi, float2 clo) {
+  if constexpr (!PK) {
+    return make_float2(div32(acc.x, fr.x, fl.x, chi.x, clo.x), div32(acc.y, fr.y, fl.y, chi.y, clo.y));
+  } else {
+    const float2 df = pk_sub(fl, fr);
+    return pk_fma(df, chi, pk_fma(df, clo, acc));
+  }
+}
+template <bool PK>
+__device__ __forceinline__ float2 upd2(float2 e0, float2 acc, float2 lam, float dthi, float dtlo) {
+  if constexpr (!PK) {
+    return make_float2(upd32(e0.x, acc.x, e0.x * lam.x, dthi, dtlo), upd32(e0.y, acc.y, e0.y * lam.y, dthi, dtlo));
+  } else {
+    const float2 nmf = pk_neg(pk_mul(e0, lam));
+    return pk_add(e0, pk_fma(nmf, make_float2(dthi, dthi), pk_fma(nmf, make_float2(dtlo, dtlo), acc)));
+  }
 }
 
 template <class T>

@@ -63,7 +63,8 @@ __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& 
 
 // nitems counts the (k,l,m) columns; the walk (ItemWalk) visits z = 0..nz-1
 // of each
-template <int NT, int R>
+// PK: the pair arithmetic on the packed f32x2 instructions (same results)
+template <int NT, int R, bool PK>
 __global__ void __launch_bounds__(NT + 32, 1)
     step_w2z_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -149,19 +150,20 @@ __global__ void __launch_bounds__(NT + 32, 1)
     float2 ec[R + 4];
 #pragma unroll
     for (int j = 0; j < R + 4; j++) ec[j] = ld2(sE + ecol[j]);
-    // ---- x faces ----
-    float fxa[R], fxb[R], fxl[R];
+    // ---- x faces: the right faces of both columns as one pair ----
+    float2 fx[R];   // (face x0+1, face x0+2)
+    float fxl[R];
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const int rb = yrow[r] * nx;
       const float2 e01 = ec[r + 2];
       const float em = sE[rb + xm];
       const float2 e23 = has_right ? ld2(sE + rb + x0 + 2) : make_float2(e01.y, e01.y);
-      fxa[r] = flux_fp32(cur.vx[r].x, cxa, em, e01.x, e01.y, e23.x);
-      fxb[r] = flux_fp32(cur.vx[r].y, cxb, e01.x, e01.y, e23.x, e23.y);
+      fx[r] = flux2<PK>(cur.vx[r], make_float2(cxa, cxb), make_float2(em, e01.x), e01, make_float2(e01.y, e23.x),
+                        e23);
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fxb[r], 1);
+    for (int r = 0; r < R; r++) fxl[r] = __shfl_up_sync(0xffffffffu, fx[r].y, 1);
     if (x0 == 0) {
 #pragma unroll
       for (int r = 0; r < R; r++) fxl[r] = open_face0_flux<float>(cur.xl[r], ec[r + 2].x);
@@ -178,47 +180,37 @@ __global__ void __launch_bounds__(NT + 32, 1)
       fy[0].x = open_face0_flux<float>(cur.yb.x, ec[2].x);
       fy[0].y = open_face0_flux<float>(cur.yb.y, ec[2].y);
     } else {
-      fy[0].x = flux_fp32(cur.yb.x, cyb, ec[0].x, ec[1].x, ec[2].x, ec[3].x);
-      fy[0].y = flux_fp32(cur.yb.y, cyb, ec[0].y, ec[1].y, ec[2].y, ec[3].y);
+      fy[0] = flux2<PK>(cur.yb, make_float2(cyb, cyb), ec[0], ec[1], ec[2], ec[3]);
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-      fy[r + 1].x = flux_fp32(cur.vy[r].x, cy[r], ec[r + 1].x, ec[r + 2].x, ec[r + 3].x, ec[r + 4].x);
-      fy[r + 1].y = flux_fp32(cur.vy[r].y, cy[r], ec[r + 1].y, ec[r + 2].y, ec[r + 3].y, ec[r + 4].y);
-    }
+    for (int r = 0; r < R; r++)
+      fy[r + 1] = flux2<PK>(cur.vy[r], make_float2(cy[r], cy[r]), ec[r + 1], ec[r + 2], ec[r + 3], ec[r + 4]);
     // ---- divergence (axis order x,y,z,k,l,m), mean-flow term, update ----
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const float2 e0 = ec[r + 2];
       const int q = yrow[r] * nx + x0;
-      float dEa = div32(0.f, fxa[r], fxl[r], hxa, oxa);
-      float dEb = div32(0.f, fxb[r], fxa[r], hxb, oxb);
-      dEa = div32(dEa, fy[r + 1].x, fy[r].x, hy[r], oy[r]);
-      dEb = div32(dEb, fy[r + 1].y, fy[r].y, hy[r], oy[r]);
+      float2 acc = div2<PK>(make_float2(0.f, 0.f), fx[r], make_float2(fxl[r], fx[r].x), make_float2(hxa, hxb),
+                            make_float2(oxa, oxb));
+      acc = div2<PK>(acc, fy[r + 1], fy[r], make_float2(hy[r], hy[r]), make_float2(oy[r], oy[r]));
 #pragma unroll
       for (int a = 2; a < 6; a++) {
         if (d.n[a] <= 1) continue;
         const float* sN = sE + (size_t)(1 + 4 * (a - 2)) * nxy + q;
         const float2 Em1 = ld2(sN + nxy), Ep1 = ld2(sN + 2 * nxy), Ep2 = ld2(sN + 3 * nxy);
-        const float2 vr = cur.vr[a - 2][r];
-        const float fra = flux_fp32(vr.x, kcr[a - 2], Em1.x, e0.x, Ep1.x, Ep2.x);
-        const float frb = flux_fp32(vr.y, kcr[a - 2], Em1.y, e0.y, Ep1.y, Ep2.y);
-        float fla, flb;
+        const float2 kc = make_float2(kcr[a - 2], kcr[a - 2]);
+        const float2 fr = flux2<PK>(cur.vr[a - 2][r], kc, Em1, e0, Ep1, Ep2);
+        float2 fl;
         if (a == 2 && wk.z > 0) {   // left z face = the previous plane's right z face
-          fla = zcarry[r].x;
-          flb = zcarry[r].y;
+          fl = zcarry[r];
         } else {
-          const float2 Em2 = ld2(sN), vl = cur.vl[a - 2][r];
-          fla = flux_fp32(vl.x, kcl[a - 2], Em2.x, Em1.x, e0.x, Ep1.x);
-          flb = flux_fp32(vl.y, kcl[a - 2], Em2.y, Em1.y, e0.y, Ep1.y);
+          const float2 Em2 = ld2(sN);
+          fl = flux2<PK>(cur.vl[a - 2][r], make_float2(kcl[a - 2], kcl[a - 2]), Em2, Em1, e0, Ep1);
         }
-        if (a == 2) zcarry[r] = make_float2(fra, frb);
-        dEa = div32(dEa, fra, fla, khr[a - 2], kor[a - 2]);
-        dEb = div32(dEb, frb, flb, khr[a - 2], kor[a - 2]);
+        if (a == 2) zcarry[r] = fr;
+        acc = div2<PK>(acc, fr, fl, make_float2(khr[a - 2], khr[a - 2]), make_float2(kor[a - 2], kor[a - 2]));
       }
-      const float mfa = e0.x * cur.lam[r].x, mfb = e0.y * cur.lam[r].y;
-      if (y0 + r < ny)
-        st2_stream(A.Enew + p0 + q, make_float2(upd32(e0.x, dEa, mfa, dthi, dtlo), upd32(e0.y, dEb, mfb, dthi, dtlo)));
+      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, upd2<PK>(e0, acc, cur.lam[r], dthi, dtlo));
     }
     mbar_arrive(&empty[s]);
     s = sn;
