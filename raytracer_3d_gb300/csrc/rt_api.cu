@@ -272,7 +272,7 @@ static cudaError_t step_once(rt_handle* h, int src, int* nlaunch) {
       FastTab T;
       for (int a = 0; a < 6; a++) T.c[a] = h->tab64 + h->toff[a];
       *nlaunch = 2;
-      return launch_step_fast(make_step_args<double>(h, src), h->split, h->mu, T, h->st);
+      return launch_step_fast(make_step_args<double>(h, src), h->split, h->mu, T, h->tune.band, h->st);
     }
     cudaError_t e = ensure_uc(h, 0);
     if (e != cudaSuccess) return e;

@@ -43,10 +43,35 @@ __device__ __forceinline__ void cell_coords(const Dims& d, long long v3, long lo
   c[5] = (int)(r / d.n[4]);
 }
 
+// resident CTAs per SM the two passes are compiled for (register budget)
+#ifndef RT_FAST_MINB_FLUX
+#define RT_FAST_MINB_FLUX 2
+#endif
+#ifndef RT_FAST_MINB_UPD
+#define RT_FAST_MINB_UPD 3
+#endif
+
 dim3 cells_grid(const Dims& d) {
   const long long bx = (d.nvol3 + 255) / 256;
   const long long by = d.nspec < 65535 ? d.nspec : 65535;
   return dim3((unsigned)bx, (unsigned)by, 1);
+}
+
+// The u-th spectral plane (k,l,m) in band order: bands of B values of m,
+// l outer inside a band, m inner, k fastest (B = 1: the natural order).
+// The CTAs that run together then read the m +-1, +-2 neighbour planes of E
+// (pass 1) and the m-1 flux planes (pass 2) from L2 instead of HBM.
+__device__ __forceinline__ long long band_plane(const Dims& d, long long u, int B) {
+  const int nk = d.n[3], nl = d.n[4], nm = d.n[5];
+  const long long per_band = (long long)nk * nl * B;
+  const long long b = u / per_band;
+  long long r = u - b * per_band;
+  const int bs = (b + 1) * B > nm ? nm - (int)b * B : B;   // the last band may be shorter
+  const int k = (int)(r % nk);
+  r /= nk;
+  const int m = (int)b * B + (int)(r % bs);
+  const int l = (int)(r / bs);
+  return k + (long long)nk * (l + (long long)nl * m);
 }
 
 // h = |v|/2 * (1 - |v*dt/d(f)|) of every face of axis a: right faces
@@ -92,11 +117,13 @@ __global__ void fast_mu_kernel(Dims d, Grid g, double dt, const double* lx, cons
 
 // pass 1: the right-face flux of every axis with n > 1 (and the face-0
 // flux at c_a = 0), one thread per cell
-__global__ void __launch_bounds__(256) fast_flux_kernel(StepArgs<double> A, SplitFluxes F) {
+__global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepArgs<double> A, SplitFluxes F,
+                                                                            int band) {
   const Dims& d = A.d;
   const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v3 >= d.nvol3) return;
-  for (long long sp = blockIdx.y; sp < d.nspec; sp += gridDim.y) {
+  for (long long u = blockIdx.y; u < d.nspec; u += gridDim.y) {
+    const long long sp = band_plane(d, u, band);
     int c[6];
     cell_coords(d, v3, sp, c);
     const long long p = v3 + sp * d.nvol3;
@@ -119,12 +146,13 @@ __global__ void __launch_bounds__(256) fast_flux_kernel(StepArgs<double> A, Spli
 }
 
 // pass 2: E_new = E*mu + sum_a c_a*(F_l - F_r), axis order x,y,z,k,l,m
-__global__ void __launch_bounds__(256) fast_update_kernel(StepArgs<double> A, SplitFluxes F, const double* mu,
-                                                          FastTab T) {
+__global__ void __launch_bounds__(256, RT_FAST_MINB_UPD) fast_update_kernel(StepArgs<double> A, SplitFluxes F,
+                                                                            const double* mu, FastTab T, int band) {
   const Dims& d = A.d;
   const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v3 >= d.nvol3) return;
-  for (long long sp = blockIdx.y; sp < d.nspec; sp += gridDim.y) {
+  for (long long u = blockIdx.y; u < d.nspec; u += gridDim.y) {
+    const long long sp = band_plane(d, u, band);
     int c[6];
     cell_coords(d, v3, sp, c);
     const long long p = v3 + sp * d.nvol3;
@@ -133,7 +161,7 @@ __global__ void __launch_bounds__(256) fast_update_kernel(StepArgs<double> A, Sp
     for (int a = 0; a < 6; a++) {
       if (d.n[a] <= 1) continue;
       const int ca = c[a];
-      const double fr = __ldcs(F.f[a] + p);
+      const double fr = F.f[a][p];   // also the left flux of cell p + s_a: kept in L2
       const double fl = ca > 0 ? F.f[a][p - d.s[a]] : F.f0[a][plane_index(d, a, c)];
       acc = __fma_rn(T.c[a][pidx(ca + 1)], __dsub_rn(fl, fr), acc);
     }
@@ -159,12 +187,13 @@ cudaError_t launch_fast_prepare(const Dims& d, const Grid& g, double dt, const d
 }
 
 cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, const double* mu, const FastTab& T,
-                             cudaStream_t st) {
+                             int band, cudaStream_t st) {
   const dim3 g = cells_grid(A.d);
-  fast_flux_kernel<<<g, 256, 0, st>>>(A, F);
+  const int B = band < 1 ? 1 : (band > A.d.n[5] ? A.d.n[5] : band);
+  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, B);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T);
+  fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, B);
   return cudaGetLastError();
 }
 

@@ -155,8 +155,9 @@ cudaError_t launch_fast_prepare(const Dims& d, const Grid& g, double dt, const d
                                 const double* const* vlo, const double* const* lam, double* const* hr,
                                 double* const* hl, double* mu, double* tab, const long long* toff,
                                 cudaStream_t st);
+// band: m values per band of the spectral-plane order (1: natural order)
 cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, const double* mu, const FastTab& T,
-                             cudaStream_t st);
+                             int band, cudaStream_t st);
 // failure-detection self-test of the bounded waits (rt_persist.cu): one CTA
 // whose waits cannot complete; raises *status, leaves *completed at 0
 cudaError_t launch_wait_probe(int* status, int* completed, cudaStream_t st);
