@@ -220,8 +220,8 @@ def fp64_peak():
             if lib.rt_fp64_rate(ctypes.byref(r)) == 0:
                 best = max(best, r.value)
     return {"fma_per_s": best, "clocks": cs.summary(),
-            "how": "rt_fp64_rate: 8 independent fma chains per thread, 8 CTAs of 256 threads per SM, "
-                   "2^14 iterations, CUDA events, best of 3"}
+            "how": "rt_fp64_rate: 8 or 16 independent fma chains per thread, 4 or 8 CTAs of 256 threads per SM, "
+                   "CUDA events on the second launch of each shape; best of 3 calls"}
 
 
 SCHEDULE_NOTES = {
