@@ -224,6 +224,9 @@ def fp64_peak():
                    "CUDA events on the second launch of each shape; best of 3 calls"}
 
 
+# committed per-cell DRAM traffic (profiles/dram_traffic.json) of each timed binary32 kernel
+FP32_TRAFFIC = {"w2z": "step_fp32_w2z", "w2p": "step_fp32_w2p", "w3": "step_fp32_w3"}
+
 SCHEDULE_NOTES = {
     "fast": "two passes without divisions (rt_fast.cu): within 1e-12 relative L-inf of the reference per step, "
             "not bit-identical",
@@ -520,7 +523,8 @@ def gpu_arm(args):
                          "ms_per_step": 1e3 * f32["seconds"] / args.steps,
                          "schedule": "%s band %d threads %d sweep %d" % tuple(f32["schedule"]),
                          "tuning_table_ms": f32["tuning_table_ms"],
-                         "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps),
+                         "roofline": roofline("fp32", f32["cells"], f32["seconds"] / args.steps,
+                                              FP32_TRAFFIC.get(f32["schedule"][0], "none")),
                          "clocks": f32["clocks"]}
     if not args.no_batch:
         forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,

@@ -27,8 +27,8 @@ def test_roofline_reports_traffic_and_source():
     sys.path.insert(0, ROOT)
     import bench
     cells = 32 ** 6
-    for key in ("step_fp64", "step_fp64_split", "step_fp32"):
-        prec = "fp32" if key.endswith("fp32") else "fp64"
+    for key in ("step_fp64", "step_fp64_split", "step_fp32_w2z"):
+        prec = "fp32" if "fp32" in key else "fp64"
         rf = bench.roofline(prec, cells, 0.5, key)
         assert rf["bound"] == "hbm" and rf["unit"] == "GB/s" and rf["traffic"] > 0
         assert rf["traffic_source"].startswith("profiles/")
