@@ -378,6 +378,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
         e1.synchronize()
     secs = e0.elapsed_time(e1) / 1e3
     b.sync()
+    launches = b.launch_count() - l0
     cells = b.cells
     error = None
     if error_steps > 0:
@@ -401,7 +402,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
                  "reference": "each member alone in binary64 (fast schedule, within 1e-12 per step of the "
                               "reference's arithmetic)"}
     out = {"value": cells * steps / secs, "unit": UNIT, "members": members, "cells_per_step": cells,
-           "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": b.launch_count() - l0,
+           "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": launches,
            "graph_steps": b.tuning[3],
            "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
                       "slice_threads": best[4], "staged_members": b.persistent_members()},
