@@ -175,25 +175,32 @@ int rt_diagnose(rt_handle* h, rt_budget* out, double* E_int, double* meanfl_int,
  * (restart.f90:15-18).  Needs a step since rt_set_state. */
 int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
 
-/* Schedule of the step kernel (no effect on results).  variant: 2 = plane
- * tiled with bulk-copy (TMA) staging of the E planes (default; used when a
- * plane of E is a multiple of 16 bytes), 3 = the same with several z planes
- * per work item (for small x-y planes), 4 = persistent CTAs that stage the
- * next item while computing the current one, 5 = persistent CTAs with one
- * producer warp feeding a ring of 2-4 staged items to `threads` consumer
- * threads that load the next item's velocities ahead, 6 = as 5 with the
- * velocities loaded at the start of each item (4-6: binary32 form; binary64
- * uses variant 2), 0 = plane tiled with plain loads, 1 = one thread per
- * cell; band: values per band of the plane schedule (default 8); threads:
- * CTA size 128, 256, 512 or 1024 (default 512; consumer threads of
- * variants 5 and 6: 128, 256 or 512).  Variants 7-14 are further forms
- * of the persistent binary32 kernel (raytracer_3d_gb300.model.Model.VARIANTS;
- * 8 = 2-wide cell blocks, 14 = the same walking whole z columns).
- * 15 = binary64 in two passes: every face flux evaluated once into flux
- * fields (allocated by this call: 48 bytes per cell plus the face-0
- * planes), then divergence and update; the binary32 form treats it as 2.
- * Shapes a variant cannot run fall back to the next one that can.  Chosen
- * by the autotuner (raytracer_3d_gb300.autotune). */
+/* Schedule of the step kernel.  variant:
+ *   2  = plane tiled with bulk-copy (TMA) staging of the E planes (default;
+ *        used when a plane of E is a multiple of 16 bytes)
+ *   3  = the same with several z planes per work item (small x-y planes)
+ *   0  = plane tiled with plain loads,  1 = one thread per cell
+ *   9  = binary32: persistent, warp-specialised, every operand staged
+ *   13 = binary32: the same for small planes, z slices per work item
+ *   14 = binary32: persistent, warp-specialised, 2-wide cell blocks, CTAs
+ *        marching along z (the production binary32 step)
+ *   17 = 14 with the cell-pair arithmetic on packed f32x2 instructions
+ *   15 = binary64 in two passes: every face flux evaluated once into flux
+ *        fields (allocated by this call: 48 bytes per cell plus the face-0
+ *        planes), then divergence and update
+ *   16 = binary64 fast: the two passes of 15 without divisions (limiter
+ *        slope selected exactly, update regrouped; 8 more bytes per cell);
+ *        within a few units in the last place of the reference's result per
+ *        step, NOT bit-identical to it.  band = m values per band of its
+ *        spectral-plane order (1: natural order)
+ * Every other variant gives the same result: bit-identical to the
+ * reference's arithmetic in binary64, and among themselves in binary32.
+ * band: values per band of the plane schedule (default 8); threads: CTA
+ * size 128, 256, 512 or 1024 (default 512; consumer threads of the
+ * persistent variants: 128, 256 or 512).  Codes 4-8 and 10-12 belonged to
+ * removed kernels and are rejected.  The binary32 form treats 15 and 16 as
+ * 2; shapes a variant cannot run fall back to the next one that can.
+ * Chosen by the autotuner (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);
 /* Sweep order of the plane schedule: 0 = bands over m (default), 1 = bands
  * over l.  No effect on results. */
