@@ -43,12 +43,15 @@ __device__ __forceinline__ void cell_coords(const Dims& d, long long v3, long lo
   c[5] = (int)(r / d.n[4]);
 }
 
-// resident CTAs per SM the two passes are compiled for (register budget)
+// resident CTAs per SM the two passes are compiled for (register budget:
+// 64 per thread).  Both passes wait on scattered loads of E and the flux
+// fields; at 32^6 four CTAs per SM measured 119 ms per step, three 128 ms,
+// two (96 registers) 157 ms
 #ifndef RT_FAST_MINB_FLUX
-#define RT_FAST_MINB_FLUX 2
+#define RT_FAST_MINB_FLUX 4
 #endif
 #ifndef RT_FAST_MINB_UPD
-#define RT_FAST_MINB_UPD 3
+#define RT_FAST_MINB_UPD 4
 #endif
 
 dim3 cells_grid(const Dims& d) {
