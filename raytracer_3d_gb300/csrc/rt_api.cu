@@ -60,6 +60,7 @@ struct rt_handle {
   double* vol3 = nullptr;       // 8 x nvol3 wavenumber integrals
   double* result = nullptr;     // DIAG_RESULT_NV doubles
   int* status = nullptr;        // device flag raised by a timed-out wait
+  unsigned* seed = nullptr;     // binary32 stochastic-rounding seeds, one per ping-pong buffer
   void* pinned = nullptr;       // host staging of one interior field
   int host_direct = 1;          // 1: the GPU reads / writes host arrays itself when the device can
   int pageable = -1;            // device supports pageable host memory access (-1: not asked yet)
@@ -220,6 +221,8 @@ static StepArgs<T> make_step_args(const rt_handle* h, int src) {
   A.dt = h->p.dt;
   A.dthi = (float)h->p.dt;
   A.dtlo = (float)(h->p.dt - (double)A.dthi);
+  A.seed_in = h->seed + src;
+  A.seed_out = h->seed + (1 - src);
   A.status = h->status;
   return A;
 }
@@ -960,6 +963,8 @@ int rt_create(const rt_dims* dims, const rt_params* params, rt_handle** out) {
   if ((rc = dev_alloc(h, (void**)&h->result, 32 * sizeof(double)))) return bail(rc);
   if ((rc = dev_alloc(h, (void**)&h->status, sizeof(int)))) return bail(rc);
   if (cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess) return bail(fail(h, RT_ERR_CUDA, "memset"));
+  if ((rc = dev_alloc(h, (void**)&h->seed, 2 * sizeof(unsigned)))) return bail(rc);
+  if (cudaMemset(h->seed, 0, 2 * sizeof(unsigned)) != cudaSuccess) return bail(fail(h, RT_ERR_CUDA, "memset"));
   *out = h;
   return RT_OK;
 }
@@ -978,6 +983,7 @@ int rt_destroy(rt_handle* h) {
   cudaFree(h->vol3);
   cudaFree(h->result);
   cudaFree(h->status);
+  cudaFree(h->seed);
   cudaFree(h->force);
   for (int a = 0; a < 6; a++) { cudaFree(h->split.f[a]); cudaFree(h->split.f0[a]); }
   cudaFree(h->mu);

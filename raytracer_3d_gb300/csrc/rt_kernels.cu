@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(256) step_kernel(StepArgs<T> A) {
     const T e0 = A.E[p];
     if constexpr (sizeof(T) == 4) {
       A.Enew[p] = cell_step32(A, p, c, e0);
+      if (blockIdx.x == 0 && sp == 0) advance_seed(A.seed_in, A.seed_out, 0);
     } else {
       const CellTerms<T> t = cell_terms<T>(A, p, c, e0);
       A.Enew[p] = update<T>(e0, t.dE, t.meanfl, A.dt);

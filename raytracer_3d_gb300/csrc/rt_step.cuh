@@ -3,6 +3,8 @@
 // mean-flow term (:202-252) and forward-Euler update (:255-268) in one
 // sweep over E.  Fluxes, dE and meanfl are never stored.
 #pragma once
+#include <cstring>
+
 #include "rt_common.cuh"
 
 namespace rt {
@@ -120,20 +122,75 @@ struct Tab32 {
 };
 
 // Divergence and update of the binary32 step.  The step accumulates
-// acc = dt * sum_a (F_l - F_r)/d_a and stores E + acc - dt*E*lambda.  The
-// constants dt/d_a and dt are carried as two-term binary32 sums (about 48
-// bits): a single rounded binary32 constant would scale every flux of an
-// axis alike, so the energy leaving through the open boundaries -- the only
-// fluxes that do not cancel in the total -- and the mean-flow exchange would
-// carry one systematic relative error of up to 2^-24 over a whole run.  With
-// the two-term constants the remaining rounding errors are unbiased and
-// average out in the total energy.
+// acc = dt * sum_a (F_l - F_r)/d_a and stores E + acc - dt*E*lambda.  Two
+// sources of systematic error are removed, so that what remains averages
+// out in the total energy:
+//  * the constants dt/d_a and dt are carried as two-term binary32 sums
+//    (about 48 bits): a single rounded binary32 constant would scale every
+//    flux of an axis alike, so the energy leaving through the open
+//    boundaries -- the only fluxes that do not cancel in the total -- and
+//    the mean-flow exchange would carry one systematic relative error of up
+//    to 2^-24 over a whole run;
+//  * the sum E + increment is rounded stochastically: to one of the two
+//    binary32 neighbours of the exact sum, the farther one with probability
+//    (distance to the nearer) / (gap).  Round-to-nearest loses every
+//    increment below half a unit in the last place of E, and where a cell's
+//    increments keep one sign (slow exchange, weak gradients) those losses
+//    add up over a run; stochastic rounding has zero mean error.  The random
+//    word is a hash of the cell's index and a per-step seed that the step
+//    kernels carry in device memory (seed_in / seed_out), so every binary32
+//    schedule, and a member of a batch or a served request, draws the same
+//    words and gives the same result bit for bit.
 __device__ __forceinline__ float div32(float acc, float fr, float fl, float chi, float clo) {
   const float df = fl - fr;
   return fmaf(df, chi, fmaf(df, clo, acc));
 }
-__device__ __forceinline__ float upd32(float e0, float acc, float mf, float dthi, float dtlo) {
-  return e0 + fmaf(-mf, dthi, fmaf(-mf, dtlo, acc));
+__host__ __device__ __forceinline__ unsigned f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  unsigned u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+__host__ __device__ __forceinline__ float f32_from_bits(unsigned u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+// counter-based random word of a cell (linear index p) at the step with `seed`
+__host__ __device__ __forceinline__ unsigned sr_bits(long long p, unsigned seed) {
+  unsigned h = ((unsigned)p ^ ((unsigned)((unsigned long long)p >> 32) * 0x85EBCA6Bu)) + seed * 0x9E3779B1u;
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return h;
+}
+// s = RN(a + b) and err = a + b - s exactly (error-free transformation of
+// the sum): the binary32 neighbour of s on the side of err with probability
+// |err| / gap, using the top 24 bits of rnd
+__host__ __device__ __forceinline__ float sr_round(float s, float err, unsigned rnd) {
+  const unsigned sb = f32_bits(s);
+  const unsigned nbits = ((err > 0.f) == ((sb >> 31) == 0u)) ? sb + 1u : sb - 1u;
+  const float nb = f32_from_bits(nbits);
+  const float gap = fabsf(nb - s);
+  const float u = (float)(rnd >> 8) * 5.9604645e-08f;   // [0, 1) in steps of 2^-24
+  return (u * gap < fabsf(err)) ? nb : s;               // err == 0: s
+}
+__host__ __device__ __forceinline__ float upd32(float e0, float acc, float mf, float dthi, float dtlo,
+                                                unsigned rnd) {
+  const float x = fmaf(-mf, dthi, fmaf(-mf, dtlo, acc));
+  const float s = e0 + x;
+  const float bp = s - e0;
+  const float err = (e0 - (s - bp)) + (x - bp);
+  return sr_round(s, err, rnd);
 }
 
 // The same per-cell arithmetic for two cells at once (flux_fp32, div32,
@@ -171,12 +228,17 @@ __device__ __forceinline__ float2 div2(float2 acc, float2 fr, float2 fl, float2 
   }
 }
 template <bool PK>
-__device__ __forceinline__ float2 upd2(float2 e0, float2 acc, float2 lam, float dthi, float dtlo) {
+__device__ __forceinline__ float2 upd2(float2 e0, float2 acc, float2 lam, float dthi, float dtlo, uint2 rnd) {
   if constexpr (!PK) {
-    return make_float2(upd32(e0.x, acc.x, e0.x * lam.x, dthi, dtlo), upd32(e0.y, acc.y, e0.y * lam.y, dthi, dtlo));
+    return make_float2(upd32(e0.x, acc.x, e0.x * lam.x, dthi, dtlo, rnd.x),
+                       upd32(e0.y, acc.y, e0.y * lam.y, dthi, dtlo, rnd.y));
   } else {
     const float2 nmf = pk_neg(pk_mul(e0, lam));
-    return pk_add(e0, pk_fma(nmf, make_float2(dthi, dthi), pk_fma(nmf, make_float2(dtlo, dtlo), acc)));
+    const float2 x = pk_fma(nmf, make_float2(dthi, dthi), pk_fma(nmf, make_float2(dtlo, dtlo), acc));
+    const float2 s = pk_add(e0, x);
+    const float2 bp = pk_sub(s, e0);
+    const float2 err = pk_add(pk_sub(e0, pk_sub(s, bp)), pk_sub(x, bp));
+    return make_float2(sr_round(s.x, err.x, rnd.x), sr_round(s.y, err.y, rnd.y));
   }
 }
 
@@ -194,8 +256,19 @@ struct StepArgs {
   const T* ucl[6];     // fp64: the same on the face-0 planes
   double dt;
   float dthi, dtlo;    // binary32 form: dt as the two-term sum dthi + dtlo
+  // binary32 form: seed of this step's stochastic rounding (read), and the
+  // next step's (written once per step by the thread that updates the
+  // field's first item: seed + 1).  Two slots per handle, swapped with E.
+  const unsigned* seed_in;
+  unsigned* seed_out;
   int* status;         // device flag: bit 0 = a bounded wait timed out
 };
+
+// the next step's seed, written by thread 0 of the CTA that takes item 0 of
+// a field (one writer per field and step; seed_in is not written by a step)
+__device__ __forceinline__ void advance_seed(const unsigned* seed_in, unsigned* seed_out, long long item) {
+  if (item == 0 && threadIdx.x == 0) *seed_out = *seed_in + 1u;
+}
 
 // Read E at cell p displaced by off along axis a from coordinate c,
 // applying the ghost-cell map (returns the mapped linear index).
@@ -301,7 +374,7 @@ __device__ __forceinline__ float cell_step32(const StepArgs<float>& A, long long
     const float fl = flux_fp32(vl, A.t32.hcfl[a][pidx(F - 1)], Em2, Em1, e0, Ep1);
     acc = div32(acc, fr, fl, A.t32.chi[a][pidx(F)], A.t32.clo[a][pidx(F)]);
   }
-  return upd32(e0, acc, e0 * A.lam[0][p], A.dthi, A.dtlo);
+  return upd32(e0, acc, e0 * A.lam[0][p], A.dthi, A.dtlo, sr_bits(p, *A.seed_in));
 }
 
 }  // namespace rt

@@ -293,6 +293,7 @@ struct W6Geom {
   int nx, ny, P, G, g, y, x0, xm, xmm;
   bool has_right, active;
   float cxa, cxb, hxa, hxb, oxa, oxb, cxl, cy, hy, oy, cyb, dthi, dtlo;
+  unsigned seed;   // this step's rounding seed of the field
 };
 
 __device__ __forceinline__ void w6_geom(const StepArgs<float>& A, int G, int t, W6Geom& w) {
@@ -326,6 +327,7 @@ __device__ __forceinline__ void w6_geom(const StepArgs<float>& A, int G, int t, 
   w.cyb = A.t32.hcfl[1][pidx(y)];
   w.dthi = A.dthi;
   w.dtlo = A.dtlo;
+  w.seed = *A.seed_in;
 }
 
 __device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& w, const W6Desc& D,
@@ -403,9 +405,11 @@ __device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& 
   }
   const float2 lam = ld2(sP + L.v(g, 10) + q);
   const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
-  if (w.active && D.z0 + g < d.n[2])
-    st2_stream(A.Enew + D.p0 + (long long)g * d.s[2] + q,
-               make_float2(upd32(e0.x, dEa, mfa, w.dthi, w.dtlo), upd32(e0.y, dEb, mfb, w.dthi, w.dtlo)));
+  if (w.active && D.z0 + g < d.n[2]) {
+    const long long p = D.p0 + (long long)g * d.s[2] + q;
+    st2_stream(A.Enew + p, make_float2(upd32(e0.x, dEa, mfa, w.dthi, w.dtlo, sr_bits(p, w.seed)),
+                                       upd32(e0.y, dEb, mfb, w.dthi, w.dtlo, sr_bits(p + 1, w.seed))));
+  }
 }
 
 // one field (mem == nullptr: A, S, nitems) or the members of an ensemble
@@ -483,6 +487,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
       w6_geom(Aj, mem ? mem[j].S.gz : S.gz, threadIdx.x, w);
       jc = j;
     }
+    advance_seed(Aj.seed_in, Aj.seed_out, mem ? it - first[j] : it);   // the field's item 0
     if (!ws_wait(&full[s], par, status)) return;
     w6_item(Aj, w, desc[s], stage0 + (size_t)s * stage_floats, lane);
     mbar_arrive(&empty[s]);

@@ -84,6 +84,12 @@ __device__ __forceinline__ void plane_item(const StepArgs<T>& A, const PlaneSche
   const Dims& d = A.d;
   const int nx = d.n[0], ny = d.n[1], nz = d.n[2], nl = d.n[4], nm = d.n[5];
   const int nxy = nx * ny;
+  // binary32: this step's rounding seed; item 0 also writes the next one
+  unsigned seed = 0;
+  if constexpr (sizeof(T) == 4) {
+    seed = *A.seed_in;
+    advance_seed(A.seed_in, A.seed_out, item);
+  }
   T* sE = reinterpret_cast<T*>(smem_raw);
   T* sFx = sE + nxy;
   T* sFy = sFx + nxy;
@@ -167,7 +173,7 @@ __device__ __forceinline__ void plane_item(const StepArgs<T>& A, const PlaneSche
       if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p)));
       st_stream(A.Enew + p, dadd(e0, dmul(A.dt, dsub(dE, mf))));
     } else {
-      st_stream(A.Enew + p, upd32(e0, dE, e0 * ld_stream(A.lam[0] + p), A.dthi, A.dtlo));
+      st_stream(A.Enew + p, upd32(e0, dE, e0 * ld_stream(A.lam[0] + p), A.dthi, A.dtlo, sr_bits(p, seed)));
     }
   }
   __syncthreads();  // shared memory is reused by the next item

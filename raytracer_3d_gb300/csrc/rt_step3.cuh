@@ -169,6 +169,12 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
   const Dims& d = A.d;
   const int nx = d.n[0], ny = d.n[1], nz = d.n[2], nl = d.n[4], nm = d.n[5];
   const int nxy = nx * ny;
+  // binary32: this step's rounding seed; item 0 also writes the next one
+  unsigned seed = 0;
+  if constexpr (sizeof(T) == 4) {
+    seed = *A.seed_in;
+    advance_seed(A.seed_in, A.seed_out, item);
+  }
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   ItemDesc<T>* desc = reinterpret_cast<ItemDesc<T>*>(smem_raw + 16);
   T* sP = reinterpret_cast<T*>(smem_raw + 16 + desc_bytes<T>());   // RT_NPLANE planes
@@ -340,7 +346,8 @@ __device__ __forceinline__ bool tma_item(const StepArgs<T>& A, const PlaneSched&
         if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + p0 + q)));
         st_stream(A.Enew + p0 + q, dadd(e0, dmul(A.dt, dsub(dE, mf))));
       } else {
-        st_stream(A.Enew + p0 + q, upd32(e0, dE, e0 * ld_stream(A.lam[0] + p0 + q), A.dthi, A.dtlo));
+        st_stream(A.Enew + p0 + q,
+                  upd32(e0, dE, e0 * ld_stream(A.lam[0] + p0 + q), A.dthi, A.dtlo, sr_bits(p0 + q, seed)));
       }
     }
   }

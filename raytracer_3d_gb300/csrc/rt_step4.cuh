@@ -62,6 +62,12 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
   const int nx = d.n[0], ny = d.n[1], nz = d.n[2], nl = d.n[4], nm = d.n[5];
   const int nxy = nx * ny;
   const int G = S.gz;
+  // binary32: this step's rounding seed; item 0 also writes the next one
+  unsigned seed = 0;
+  if constexpr (sizeof(T) == 4) {
+    seed = *A.seed_in;
+    advance_seed(A.seed_in, A.seed_out, item);
+  }
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   GroupDesc<T>* desc = reinterpret_cast<GroupDesc<T>*>(smem_raw + 16);
   T* sW = reinterpret_cast<T*>(smem_raw + 16 + gdesc_bytes<T>());  // z window, G+4 planes
@@ -284,7 +290,7 @@ __device__ __forceinline__ bool group_item(const StepArgs<T>& A, const PlaneSche
       if (nz > 1) mf = dadd(mf, dmul(e0, ld_stream(A.lam[2] + pc)));
       st_stream(A.Enew + pc, dadd(e0, dmul(A.dt, dsub(dE, mf))));
     } else {
-      st_stream(A.Enew + pc, upd32(e0, dE, e0 * ld_stream(A.lam[0] + pc), A.dthi, A.dtlo));
+      st_stream(A.Enew + pc, upd32(e0, dE, e0 * ld_stream(A.lam[0] + pc), A.dthi, A.dtlo, sr_bits(pc, seed)));
     }
   }
   __syncthreads();

@@ -122,6 +122,8 @@ __global__ void __launch_bounds__(NT + 32, 1)
     ecol[j] = yy * nx + x0;
   }
   const float dthi = A.dthi, dtlo = A.dtlo;
+  const unsigned seed = *A.seed_in;            // this step's rounding seed
+  advance_seed(A.seed_in, A.seed_out, blockIdx.x);   // CTA 0 takes column 0
 
   W2Regs<R> cur;
   int s = 0;
@@ -210,7 +212,9 @@ __global__ void __launch_bounds__(NT + 32, 1)
         if (a == 2) zcarry[r] = fr;
         acc = div2<PK>(acc, fr, fl, make_float2(khr[a - 2], khr[a - 2]), make_float2(kor[a - 2], kor[a - 2]));
       }
-      if (y0 + r < ny) st2_stream(A.Enew + p0 + q, upd2<PK>(e0, acc, cur.lam[r], dthi, dtlo));
+      if (y0 + r < ny)
+        st2_stream(A.Enew + p0 + q, upd2<PK>(e0, acc, cur.lam[r], dthi, dtlo,
+                                             make_uint2(sr_bits(p0 + q, seed), sr_bits(p0 + q + 1, seed))));
     }
     mbar_arrive(&empty[s]);
     s = sn;

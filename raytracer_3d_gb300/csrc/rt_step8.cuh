@@ -212,6 +212,7 @@ struct W3Geom {
   int yrow[R], ecol[R + 4];
   float cxa, cxb, hxa, hxb, oxa, oxb, cxl, cyb, dthi, dtlo;
   float cy[R], hy[R], oy[R];
+  unsigned seed;   // this step's rounding seed of the field
 };
 
 template <int R>
@@ -255,6 +256,7 @@ __device__ __forceinline__ void w3_geom(const StepArgs<float>& A, int t, W3Geom<
                      : RT_W3_VY * g.nxy + ((y0 - 1 < ny - 1 ? y0 - 1 : ny - 1)) * nx + x0;
   g.dthi = A.dthi;
   g.dtlo = A.dtlo;
+  g.seed = *A.seed_in;
 }
 
 // one item of one consumer thread from a filled stage
@@ -343,8 +345,8 @@ __device__ __forceinline__ void w3_item(const StepArgs<float>& A, const W3Geom<R
     const float2 lam = ld2(sE + RT_W3_LAM * nxy + q);
     const float mfa = e0.x * lam.x, mfb = e0.y * lam.y;
     if (y0 + r < ny)
-      st2_stream(A.Enew + p0 + q,
-                 make_float2(upd32(e0.x, dEa, mfa, g.dthi, g.dtlo), upd32(e0.y, dEb, mfb, g.dthi, g.dtlo)));
+      st2_stream(A.Enew + p0 + q, make_float2(upd32(e0.x, dEa, mfa, g.dthi, g.dtlo, sr_bits(p0 + q, g.seed)),
+                                              upd32(e0.y, dEb, mfb, g.dthi, g.dtlo, sr_bits(p0 + q + 1, g.seed))));
   }
 }
 
@@ -390,6 +392,7 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
   const int lane = threadIdx.x & 31;
   W3Geom<R> g;
   w3_geom<R>(A, threadIdx.x, g);
+  advance_seed(A.seed_in, A.seed_out, blockIdx.x);   // CTA 0 takes item 0
   int s = 0;
   uint32_t par = 0;
   for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -458,6 +461,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
       w3_geom<R>(A, threadIdx.x, g);
       jc = j;
     }
+    advance_seed(A.seed_in, A.seed_out, it - first[j]);   // the member's item 0
     if (!ws_wait(&full[s], par, status)) return;
     w3_item<R>(A, g, desc[s], stage0 + (size_t)s * stage_floats, lane);
     mbar_arrive(&empty[s]);

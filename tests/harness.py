@@ -118,3 +118,25 @@ def error_norms(got, ref):
         dmax = max(dmax, float(np.max(np.abs(d))))
         rmax = max(rmax, float(np.max(np.abs(r))))
     return (num2 ** 0.5) / (den2 ** 0.5), dmax / rmax
+
+
+def rounding_noise_bound(E, widths, steps, sigmas=4.0):
+    """drift allowance from the binary32 update's unbiased rounding noise:
+    each step rounds every cell to one of its two binary32 neighbours with
+    zero mean error and a standard deviation of at most 2^-23/sqrt(6) of the
+    cell's value, independently, so the total energy drifts as a random walk
+    of relative standard deviation 2^-23/sqrt(6) * sqrt(steps / N_eff), with
+    N_eff = (sum E vol)^2 / sum (E vol)^2 the effective number of cells
+    carrying the energy.  Returns sigmas of that deviation."""
+    v5 = np.ones([len(w) for w in widths[:5]])
+    for a in range(5):
+        shp = [1] * 5
+        shp[a] = len(widths[a])
+        v5 = v5 * widths[a].reshape(shp)
+    s1 = s2 = 0.0
+    for m in range(E.shape[5]):
+        ev = np.asarray(E[..., m], dtype=np.float64) * v5 * float(widths[5][m])
+        s1 += float(np.sum(ev))
+        s2 += float(np.sum(ev * ev))
+    n_eff = s1 * s1 / s2
+    return sigmas * 2.0 ** -23 / 6 ** 0.5 * (steps / n_eff) ** 0.5

@@ -12,7 +12,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from harness import ONX, build_oracle, configs, face_range, interior, max_rel
+from harness import ONX, build_oracle, configs, face_range, interior, max_rel, rounding_noise_bound
 
 pytestmark = pytest.mark.gpu
 
@@ -137,6 +137,10 @@ def test_fast_fp64_switches_with_bit_exact_schedules():
                 assert np.array_equal(m.E[sl], o.E[sl]), sched
     finally:
         m.close()
+
+
+def vol_widths(o, n):
+    return [o.grid["xyzklm"[a]]["dt"][ONX:ONX + n[a]] for a in range(6)]
 
 
 def _vol(o, n):
@@ -341,12 +345,17 @@ def test_fp32_persistent_matches_tma(n, tuning):
 @pytest.mark.parametrize("variant", ["tma", "group", "plane", "w3", "w6", "w2z", "w2p", "cell"])
 def test_fp32_form_against_fp64_oracle(variant):
     """binary32 state/fluxes/velocities with binary64 coefficients: error
-    after 200 steps of the all-axes shear case."""
+    after 200 steps of the all-axes shear case, both from the initial state
+    rounded to binary32 (the input both forms hold exactly).  On this small
+    field (1.1e5 cells) the unbiased rounding noise of the binary32 update
+    is itself of order 1e-9 over 200 steps, so the drift is held to 1e-9 or
+    4 standard deviations of that noise, whichever is larger."""
     exp = configs.shear_mini(n=(8, 6, 8, 6, 6, 8))
     m = configs.build_model(exp, "fp32")
     m.set_tuning(variant)
     o = build_oracle(exp)
     sl = interior(exp.n)
+    o.E[sl] = o.E[sl].astype(np.float32).astype(np.float64)
     try:
         assert m.dt == o.dt
         m.integrate(200)
@@ -357,10 +366,12 @@ def test_fp32_form_against_fp64_oracle(variant):
         l2 = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
         linf = max_rel(got, ref)
         drift = abs(_energy(got, o, exp.n) - _energy(ref, o, exp.n)) / abs(_energy(ref, o, exp.n))
-        print("fp32 vs fp64 oracle after 200 steps: L2 %.3e Linf %.3e energy %.3e" % (l2, linf, drift))
+        noise = rounding_noise_bound(ref, vol_widths(o, exp.n), 200)
+        print("fp32 vs fp64 oracle after 200 steps: L2 %.3e Linf %.3e energy %.3e (noise allowance %.2e)"
+              % (l2, linf, drift, noise))
         assert l2 <= 1e-5
         assert linf <= 1e-4
-        assert drift <= 1e-9
+        assert drift <= max(1e-9, noise)
     finally:
         m.close()
 

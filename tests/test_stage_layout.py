@@ -50,3 +50,19 @@ def test_fast_superbee_selection_is_exact():
         print(r.stdout)
         assert r.returncode == 0, r.stdout + r.stderr
         assert " 0 failures" in r.stdout
+
+
+def test_binary32_update_rounds_without_bias():
+    """the binary32 update's stochastic rounding returns a neighbour of the
+    exact sum and has zero mean error over the random words, also for
+    increments far below half a unit in the last place"""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "sr_round_check")
+        cmd = [_nvcc(), "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC,
+               os.path.join(HERE, "native", "sr_round_check.cu"), "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+        print(r.stdout)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert " 0 failures" in r.stdout
