@@ -80,6 +80,8 @@ inline bool w3_ok(const Dims& d, int threads) {
 
 // rt_persist_w2.cu (the caller checks w2_ok first)
 // packed: the cell-pair arithmetic on the f32x2 instructions (same results)
-cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool packed, cudaStream_t st);
+// prefetch: the next plane's operands into L2 (the packed form only)
+cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool packed, bool prefetch,
+                       cudaStream_t st);
 
 }  // namespace rt

@@ -61,10 +61,41 @@ __device__ __forceinline__ void w2_load(const StepArgs<float>& A, const WsDesc& 
                  : (y0 < ny ? ld2(A.vel[1] + p0 + (long long)(y0 - 1) * nx + x0) : make_float2(0.f, 0.f));
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+// The next item of a z column is the next z plane: every per-cell operand of
+// the consumer (velocities, growth rate; the left-face bases of k, l, m move
+// with z as well) lies one plane (nx*ny values) further on.  Asking L2 for
+// those lines now turns the next item's loads from HBM latency into L2
+// latency, without holding anything in registers.
+template <int R>
+__device__ __forceinline__ void w2_prefetch_next(const StepArgs<float>& A, const WsDesc& D, int x0,
+                                                 const int yrow[R]) {
+  const Dims& d = A.d;
+  const int nx = d.n[0];
+  const long long nxy = (long long)nx * d.n[1];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int q = yrow[r] * nx + x0;
+    const long long o = D.p0 + nxy + q;
+    prefetch_l2(A.vel[0] + o);
+    prefetch_l2(A.vel[1] + o);
+    prefetch_l2(A.lam[0] + o);
+#pragma unroll
+    for (int a = 2; a < 6; a++) {
+      if (d.n[a] <= 1) continue;
+      prefetch_l2(A.vel[a] + o);
+      if (a > 2) prefetch_l2(D.vl[a - 2] + nxy + q);
+    }
+  }
+}
+
 // nitems counts the (k,l,m) columns; the walk (ItemWalk) visits z = 0..nz-1
 // of each
-// PK: the pair arithmetic on the packed f32x2 instructions (same results)
-template <int NT, int R, bool PK>
+// PK: the pair arithmetic on the packed f32x2 instructions (same results);
+// PFN: prefetch the next plane's operands into L2 (no effect on results)
+template <int NT, int R, bool PK, bool PFN = false>
 __global__ void __launch_bounds__(NT + 32, 1)
     step_w2z_kernel(StepArgs<float> A, PlaneSched S, long long nitems, int ns) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,6 +167,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
     if (sn == ns) { sn = 0; parn ^= 1u; }
     if (!ws_wait(&dful[s], par, A.status)) return;
     w2_load<R>(A, desc[s], x0, y0, yrow, lane, cur, wk.z > 0);
+    if (PFN && wk.z + 1 < d.n[2]) w2_prefetch_next<R>(A, desc[s], x0, yrow);
     const WsDesc& D = desc[s];
     const long long p0 = D.p0;
     float kcr[4], khr[4], kor[4], kcl[4];
