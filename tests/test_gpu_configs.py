@@ -7,7 +7,11 @@
   held to 1e-12 per step of the reference's arithmetic): relative L2
   <= 1e-5 and relative total-energy drift <= 1e-9.
 * the 48-member binary32 ensemble, 500 steps in one batch, against every
-  member run alone in binary64: the same bounds per member.
+  member run alone in binary64: L2 <= 1e-5 per member; the energy drift of
+  the ensemble and of every member within 1e-9 or four standard deviations
+  of the binary32 update's unbiased rounding noise, whichever is larger (a
+  member of 8^3 x 8^3 cells whose packet covers a few thousand cells has a
+  noise of a few 1e-9 over 500 steps).
 
 These runs hold up to about 210 GB of device memory and take minutes; each
 binary64 handle is closed before the binary32 one is built."""
@@ -135,7 +139,7 @@ def test_config4_ensemble_500_steps_against_fp64():
         for m in models:
             m.close()
     worst = {"l2": 0.0, "linf": 0.0, "drift": 0.0, "excess": 0.0}
-    tot32 = tot64 = 0.0
+    tot32 = tot64 = var = 0.0
     for e, g, w in zip(exps, got, weights):
         m = configs.build_model(e, "fp64", padded=False)
         try:
@@ -150,16 +154,22 @@ def test_config4_ensemble_500_steps_against_fp64():
         e64, e32 = energy_sum(ref, w), energy_sum(g, w)
         tot32 += e32
         tot64 += e64
+        noise = rounding_noise_bound(ref, w, steps)        # 4 standard deviations, relative
+        var += (noise / 4 * e64) ** 2
         drift = abs(e32 - e64) / abs(e64)
         worst["l2"] = max(worst["l2"], l2)
         worst["linf"] = max(worst["linf"], linf)
         worst["drift"] = max(worst["drift"], drift)
         # a small member's own unbiased rounding noise may exceed 1e-9
-        worst["excess"] = max(worst["excess"], drift / max(FP32_DRIFT_TOL, rounding_noise_bound(ref, w, steps)))
+        worst["excess"] = max(worst["excess"], drift / max(FP32_DRIFT_TOL, noise))
     ens = abs(tot32 - tot64) / abs(tot64)
-    print("48-member ensemble, %d steps, binary32 batch against binary64 alone: ensemble energy %.3e; "
-          "worst member L2 %.3e  Linf %.3e  energy %.3e (%.2f of its allowance)"
-          % (steps, ens, worst["l2"], worst["linf"], worst["drift"], worst["excess"]))
+    # the ensemble's own rounding noise: the members' independent deviations
+    # add in quadrature, weighted by their energies (the small members carry
+    # most of it: a packet of a few cells per axis on a coarse grid)
+    ens_noise = 4 * var ** 0.5 / abs(tot64)
+    print("48-member ensemble, %d steps, binary32 batch against binary64 alone: ensemble energy %.3e "
+          "(noise allowance %.2e); worst member L2 %.3e  Linf %.3e  energy %.3e (%.2f of its allowance)"
+          % (steps, ens, ens_noise, worst["l2"], worst["linf"], worst["drift"], worst["excess"]))
     assert worst["l2"] <= FP32_L2_TOL
-    assert ens <= FP32_DRIFT_TOL
+    assert ens <= max(FP32_DRIFT_TOL, ens_noise)
     assert worst["excess"] <= 1.0
