@@ -74,14 +74,16 @@ __host__ __device__ __forceinline__ double superbee_slope64(double Rj, double up
   return f64_from_bits(m | s);
 }
 
-// p ? a : b as one select instruction the compiler cannot move arithmetic
-// through: the upwind difference is formed from the selected operands, one
-// binary64 subtraction, instead of both differences and a select of them
+// p ? a : b formed on the integer pipes as b ^ ((a ^ b) & mask) with a mask
+// the compilers cannot see through, so the upwind difference is one binary64
+// subtraction of the selected operands -- without the opaque mask both
+// differences get formed and one of them selected, a third binary64
+// subtraction per face
 __device__ __forceinline__ double sel64(bool p, double a, double b) {
-  double r;
-  asm("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %3, 0;\n\tselp.f64 %0, %1, %2, q;\n\t}"
-      : "=d"(r) : "d"(a), "d"(b), "r"((int)p));
-  return r;
+  unsigned long long m = 0ull - (unsigned long long)p;   // all ones when p
+  asm("mov.b64 %0, %0;" : "+l"(m));
+  const unsigned long long ua = f64_bits(a), ub = f64_bits(b);
+  return f64_from_bits(ub ^ ((ua ^ ub) & m));
 }
 
 // binary64 face flux of the fast form, face between Eb = E0 and Ec = Ep1
