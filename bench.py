@@ -209,7 +209,7 @@ def time_steps(model, steps):
     return e0.elapsed_time(e1) / 1e3, model.launch_count() - l0
 
 
-FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w2p", "w2q", "w3", "w6") for t in (128, 256, 512) for b in (4, 8)
+FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w2q", "w3", "w6") for t in (128, 256, 512) for b in (4, 8)
                     for s in (0, 1)]
                    + [("tma", b, t, s) for t in (256, 512, 1024) for b in (4, 8) for s in (0, 1)])
 
@@ -257,7 +257,7 @@ def fp64_peak():
 
 
 # committed per-cell DRAM traffic (profiles/dram_traffic.json) of each timed binary32 kernel
-FP32_TRAFFIC = {"w2z": "step_fp32_w2z", "w2p": "step_fp32_w2p", "w3": "step_fp32_w3"}
+FP32_TRAFFIC = {"w2z": "step_fp32_w2z", "w2q": "step_fp32_w2q", "w3": "step_fp32_w3"}
 
 SCHEDULE_NOTES = {
     "fast": "two passes without divisions (rt_fast.cu): within 1e-12 relative L-inf of the reference per step, "
@@ -642,7 +642,7 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--n", type=int, default=32, help="cube size of the workload (profiling of small cases)")
     ap.add_argument("--dims", default=None, help="nx,ny,nz,nk,nl,nm of a profiling case (with --no-fp64)")
-    ap.add_argument("--variant", default="tma", choices=("w2z", "w2p", "w2q", "w6", "w3", "tma", "group", "plane", "cell"))
+    ap.add_argument("--variant", default="tma", choices=("w2z", "w2q", "w6", "w3", "tma", "group", "plane", "cell"))
     ap.add_argument("--fp64-variant", default=None, choices=("tma", "split", "fast"),
                     help="binary64 schedule (default: the fastest of the candidates by dry steps)")
     ap.add_argument("--band", type=int, default=8)

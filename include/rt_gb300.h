@@ -183,8 +183,10 @@ int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
  *   9  = binary32: persistent, warp-specialised, every operand staged
  *   13 = binary32: the same for small planes, z slices per work item
  *   14 = binary32: persistent, warp-specialised, 2-wide cell blocks, CTAs
- *        marching along z (the production binary32 step)
- *   17 = 14 with the cell-pair arithmetic on packed f32x2 instructions
+ *        marching along z
+ *   18 = 14 with the cell-pair arithmetic on packed f32x2 instructions and
+ *        the next plane's operands prefetched into L2 (the production
+ *        binary32 step)
  *   15 = binary64 in two passes: every face flux evaluated once into flux
  *        fields (allocated by this call: 48 bytes per cell plus the face-0
  *        planes), then divergence and update
@@ -197,8 +199,8 @@ int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
  * reference's arithmetic in binary64, and among themselves in binary32.
  * band: values per band of the plane schedule (default 8); threads: CTA
  * size 128, 256, 512 or 1024 (default 512; consumer threads of the
- * persistent variants: 128, 256 or 512).  Codes 4-8 and 10-12 belonged to
- * removed kernels and are rejected.  The binary32 form treats 15 and 16 as
+ * persistent variants: 128, 256 or 512).  Codes 4-8, 10-12 and 17 belonged
+ * to removed kernels and are rejected.  The binary32 form treats 15 and 16 as
  * 2; shapes a variant cannot run fall back to the next one that can.
  * Chosen by the autotuner (raytracer_3d_gb300.autotune). */
 int rt_set_tuning(rt_handle* h, int variant, int band, int threads);

@@ -14,14 +14,14 @@ import time
 
 DEFAULT_CANDIDATES = [
     (variant, band, threads, sweep)
-    for variant in ("w2z", "w2p", "w2q", "w3", "w6", "tma", "group", "plane")
+    for variant in ("w2z", "w2q", "w3", "w6", "tma", "group", "plane")
     for threads in (128, 256, 512, 1024)
     for band in (4, 8, 16)
     for sweep in (0, 1)
     if not (variant == "plane" and threads == 1024)
-    and not (variant in ("w2z", "w2p", "w2q", "w3", "w6") and threads == 1024)
+    and not (variant in ("w2z", "w2q", "w3", "w6") and threads == 1024)
     and not (variant == "w6" and threads == 128)
-    and not (variant not in ("w2z", "w2p", "w2q", "w3") and threads == 128)
+    and not (variant not in ("w2z", "w2q", "w3") and threads == 128)
 ]
 
 

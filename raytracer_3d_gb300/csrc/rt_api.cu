@@ -1520,7 +1520,7 @@ int rt_set_tuning(rt_handle* h, int variant, int band, int threads) {
   if (!h) return RT_ERR_ARG;
   if (variant != RT_VARIANT_PLANE && variant != RT_VARIANT_CELL && variant != RT_VARIANT_TMA &&
       variant != RT_VARIANT_GROUP && variant != RT_VARIANT_W3 && variant != RT_VARIANT_W6 &&
-      variant != RT_VARIANT_W2Z && variant != RT_VARIANT_W2P && variant != RT_VARIANT_W2Q &&
+      variant != RT_VARIANT_W2Z && variant != RT_VARIANT_W2Q &&
       variant != RT_VARIANT_SPLIT &&
       variant != RT_VARIANT_FAST)
     return fail(h, RT_ERR_ARG, "rt_set_tuning: unknown variant %d", variant);

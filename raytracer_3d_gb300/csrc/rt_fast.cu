@@ -120,8 +120,9 @@ __global__ void fast_mu_kernel(Dims d, Grid g, double dt, const double* lx, cons
 
 // pass 1: the right-face flux of every axis with n > 1 (and the face-0
 // flux at c_a = 0), one thread per cell
+// ones: ~0 (see sel64)
 __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepArgs<double> A, SplitFluxes F,
-                                                                            int band) {
+                                                                            int band, unsigned long long ones) {
   const Dims& d = A.d;
   const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v3 >= d.nvol3) return;
@@ -138,11 +139,11 @@ __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepA
       const double Em1 = A.E[nb_index(d, p, a, ca, -1, c[5])];
       const double Ep1 = A.E[nb_index(d, p, a, ca, +1, c[5])];
       const double Ep2 = A.E[nb_index(d, p, a, ca, +2, c[5])];
-      __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2));
+      __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2, ones));
       if (ca == 0) {  // face 0: E(-2), E(-1), E(0), E(1) through the boundary maps
         const long long q = plane_index(d, a, c);
         const double Em2 = A.E[nb_index(d, p, a, ca, -2, c[5])];
-        F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1);
+        F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1, ones);
       }
     }
   }
@@ -193,7 +194,7 @@ cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, co
                              int band, cudaStream_t st) {
   const dim3 g = cells_grid(A.d);
   const int B = band < 1 ? 1 : (band > A.d.n[5] ? A.d.n[5] : band);
-  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, B);
+  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, B, ~0ull);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, B);

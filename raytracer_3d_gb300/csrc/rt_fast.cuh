@@ -74,14 +74,14 @@ __host__ __device__ __forceinline__ double superbee_slope64(double Rj, double up
   return f64_from_bits(m | s);
 }
 
-// p ? a : b formed on the integer pipes as b ^ ((a ^ b) & mask) with a mask
-// the compilers cannot see through, so the upwind difference is one binary64
-// subtraction of the selected operands -- without the opaque mask both
-// differences get formed and one of them selected, a third binary64
-// subtraction per face
-__device__ __forceinline__ double sel64(bool p, double a, double b) {
-  unsigned long long m = 0ull - (unsigned long long)p;   // all ones when p
-  asm("mov.b64 %0, %0;" : "+l"(m));
+// p ? a : b formed on the integer pipes as b ^ ((a ^ b) & mask), the mask
+// ANDed with `ones`, a kernel argument that is always all ones but unknown
+// to the compilers: the upwind difference then stays one binary64
+// subtraction of the selected operands.  A select the compilers can see
+// becomes both differences and a select of them, a third binary64
+// subtraction per face.
+__device__ __forceinline__ double sel64(bool p, double a, double b, unsigned long long ones) {
+  const unsigned long long m = (0ull - (unsigned long long)p) & ones;   // all ones when p
   const unsigned long long ua = f64_bits(a), ub = f64_bits(b);
   return f64_from_bits(ub ^ ((ua ^ ub) & m));
 }
@@ -91,11 +91,11 @@ __device__ __forceinline__ double sel64(bool p, double a, double b) {
 // and h its cached |v|/2*(1-|v dt/d|): two subtractions, one multiply, one
 // fma on the binary64 pipe
 __device__ __forceinline__ double flux_fast64(double v, double h, double Em1, double E0, double Ep1,
-                                              double Ep2) {
+                                              double Ep2, unsigned long long ones) {
   const bool pos = f64_pos(v);
   const double Rj = __dsub_rn(Ep1, E0);
-  const double up = __dsub_rn(sel64(pos, E0, Ep2), sel64(pos, Em1, Ep1));
-  const double Eu = sel64(pos, E0, Ep1);
+  const double up = __dsub_rn(sel64(pos, E0, Ep2, ones), sel64(pos, Em1, Ep1, ones));
+  const double Eu = sel64(pos, E0, Ep1, ones);
   return __fma_rn(h, superbee_slope64(Rj, up), __dmul_rn(v, Eu));
 }
 

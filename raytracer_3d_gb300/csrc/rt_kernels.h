@@ -69,9 +69,9 @@ cudaError_t launch_lam_combine(const double* lx, const double* ly, const double*
 #define RT_VARIANT_GROUP 3
 #define RT_VARIANT_W3 9       // binary32: every operand staged by TMA
 #define RT_VARIANT_W6 13      // binary32: small planes, z slices per item
-#define RT_VARIANT_W2Z 14     // binary32 production step: 2-wide blocks, z-march
-#define RT_VARIANT_W2P 17     // the same with the cell-pair arithmetic on packed f32x2 instructions
-#define RT_VARIANT_W2Q 18     // 17 with the next plane's operands prefetched into L2
+#define RT_VARIANT_W2Z 14     // binary32: 2-wide blocks, z-march
+#define RT_VARIANT_W2Q 18     // the same with the cell-pair arithmetic on packed f32x2 instructions and
+                              // the next plane's operands prefetched into L2 (the binary32 production step)
 #define RT_VARIANT_SPLIT 15   // binary64: every face flux once, two passes (rt_split.cu)
 #define RT_VARIANT_FAST 16    // binary64: two passes without divisions (rt_fast.cu), within 1e-12 of the reference
 struct StepTuning {

@@ -216,12 +216,11 @@ cudaError_t launch_persist(const StepArgs<float>& A, const StepTuning& tn, cudaS
     if (tn.threads == 256) return launch_w3_nt<256>(A, S, st);
     return launch_w3_nt<512>(A, S, st);
   }
-  if ((tn.variant == RT_VARIANT_W2Z || tn.variant == RT_VARIANT_W2P || tn.variant == RT_VARIANT_W2Q) &&
-      w2_ok(A.d, tn.threads)) {
+  if ((tn.variant == RT_VARIANT_W2Z || tn.variant == RT_VARIANT_W2Q) && w2_ok(A.d, tn.threads)) {
     done = true;
     // columns of z in band order over (k,l,m): units are k alone (gz = nz)
     const PlaneSched S = make_sched(A.d, tn, A.d.n[2]);
-    return launch_w2z(A, S, tn.threads, tn.variant != RT_VARIANT_W2Z, tn.variant == RT_VARIANT_W2Q, st);
+    return launch_w2z(A, S, tn.threads, tn.variant == RT_VARIANT_W2Q, st);
   }
   return cudaSuccess;
 }

@@ -80,8 +80,8 @@ inline bool w3_ok(const Dims& d, int threads) {
 
 // rt_persist_w2.cu (the caller checks w2_ok first)
 // packed: the cell-pair arithmetic on the f32x2 instructions (same results)
-// prefetch: the next plane's operands into L2 (the packed form only)
-cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool packed, bool prefetch,
-                       cudaStream_t st);
+// tuned: the packed f32x2 arithmetic with the next plane's operands
+// prefetched into L2 (RT_VARIANT_W2Q); else the scalar form (RT_VARIANT_W2Z)
+cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool tuned, cudaStream_t st);
 
 }  // namespace rt

@@ -1,6 +1,7 @@
 // rt_persist_w2.cu -- launcher of the production binary32 step kernel
-// (rt_step7.cuh, RT_VARIANT_W2Z: 2-wide blocks, CTAs marching along z over
-// the (k,l,m) columns).
+// (rt_step7.cuh: 2-wide blocks, CTAs marching along z over the (k,l,m)
+// columns; RT_VARIANT_W2Q with packed pair arithmetic and L2 prefetch of
+// the next plane, RT_VARIANT_W2Z the scalar form without prefetch).
 #include "rt_persist.cuh"
 
 namespace rt {
@@ -39,10 +40,8 @@ cudaError_t launch_w2z_pk(const StepArgs<float>& A, const PlaneSched& S, int thr
 
 }  // namespace
 
-cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool packed, bool prefetch,
-                       cudaStream_t st) {
-  if (packed && prefetch) return launch_w2z_pk<true, true>(A, S, threads, st);
-  return packed ? launch_w2z_pk<true, false>(A, S, threads, st) : launch_w2z_pk<false, false>(A, S, threads, st);
+cudaError_t launch_w2z(const StepArgs<float>& A, const PlaneSched& S, int threads, bool tuned, cudaStream_t st) {
+  return tuned ? launch_w2z_pk<true, true>(A, S, threads, st) : launch_w2z_pk<false, false>(A, S, threads, st);
 }
 
 }  // namespace rt

@@ -259,8 +259,8 @@ class Model:
         return {k: getattr(b, k) for k in _lib.BUDGET_FIELDS}, arrs
 
     # ---- plumbing ---------------------------------------------------------------
-    # rt_set_tuning codes (4-8 and 10-12 belonged to removed binary32 kernels)
-    VARIANTS = {"plane": 0, "cell": 1, "tma": 2, "group": 3, "w3": 9, "w6": 13, "w2z": 14, "split": 15, "fast": 16, "w2p": 17, "w2q": 18}
+    # rt_set_tuning codes (4-8, 10-12 and 17 belonged to removed binary32 kernels)
+    VARIANTS = {"plane": 0, "cell": 1, "tma": 2, "group": 3, "w3": 9, "w6": 13, "w2z": 14, "split": 15, "fast": 16, "w2q": 18}
 
     def set_tuning(self, variant="tma", band=8, threads=512, sweep=0):
         """Schedule of the step kernel; never changes results."""
