@@ -3,7 +3,8 @@
 Workload (N=1): the 32^3 x 32^3 wave field with a mean flow
 U = 0.1 sin(2 pi y/Ly) exp(z/500), log-normal spectrum, CFL 0.4, plain
 binary64 form (1,073,741,824 cells per step).  A step is one forward-Euler
-time step of the whole field (one launch of the fused step kernel).
+time step of the whole field with the schedule the autotuner picks (the
+division-free two-pass step: flux pass and update pass, two launches).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -570,8 +571,9 @@ def gpu_arm(args):
                                               FP32_TRAFFIC.get(f32["schedule"][0], "none")),
                          "clocks": f32["clocks"]}
     if not args.no_batch:
-        forms["fp32_batched"] = bench_batched(args.batch_steps, args.warmup, members=args.batch_members,
-                                              error_steps=args.batch_error_steps)
+        forms["fp32_batched"] = bench_batched(
+            args.batch_steps, args.warmup, members=args.batch_members, error_steps=args.batch_error_steps,
+            fixed=tuple(int(v) for v in args.batch_tuning.split(",")) if args.batch_tuning else None)
     if not args.no_serve:
         forms["serving"] = bench_serving(nreq=args.serve_requests)
     cells = main["cells"]
@@ -656,7 +658,7 @@ def main():
     ap.add_argument("--batch-members", type=int, default=48)
     ap.add_argument("--batch-spatial", default=None, help="spatial extents of the members, e.g. 8,16 (profiling)")
     ap.add_argument("--batch-tuning", default=None,
-                    help="band,threads,sweep,persistent[,slices] (skip the batch tuner)")
+                    help="band,threads,sweep,persistent[,slices]: a fixed batch schedule instead of the batch tuner")
     ap.add_argument("--only", default="all", choices=("all", "batch", "serve"),
                     help="batch / serve: that form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)

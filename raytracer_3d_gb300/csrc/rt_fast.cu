@@ -32,49 +32,107 @@ namespace rt {
 
 namespace {
 
-__device__ __forceinline__ void cell_coords(const Dims& d, long long v3, long long sp, int c[6]) {
-  c[0] = (int)(v3 % d.n[0]);
-  long long r = v3 / d.n[0];
-  c[1] = (int)(r % d.n[1]);
-  c[2] = (int)(r / d.n[1]);
-  c[3] = (int)(sp % d.n[3]);
-  r = sp / d.n[3];
-  c[4] = (int)(r % d.n[4]);
-  c[5] = (int)(r / d.n[4]);
+// Division of a 32-bit index n < 2^31 by a divisor fixed for the launch:
+// q = (n * m) >> S with S = 31 + ceil(log2 d) and m = ceil(2^S / d) < 2^32
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994: the rounding error n*(m - 2^S/d)/2^S stays
+// below 1/d for n < 2^31, so the quotient is exact).  One wide multiply
+// and one shift instead of a generic division sequence per coordinate.
+struct DivU32 {
+  unsigned d, m, S;
+  __device__ __forceinline__ unsigned div(unsigned n) const {
+    return (unsigned)(((unsigned long long)n * m) >> S);
+  }
+};
+
+DivU32 make_div(unsigned d) {
+  unsigned k = 0;
+  while ((1ull << k) < d) k++;
+  const unsigned S = 31 + k;
+  const unsigned long long m = ((1ull << S) + d - 1) / d;
+  return DivU32{d, (unsigned)m, S};
 }
 
-// resident CTAs per SM the two passes are compiled for (register budget:
-// 64 per thread).  Both passes wait on scattered loads of E and the flux
-// fields; at 32^6 four CTAs per SM measured 119 ms per step, three 128 ms,
-// two (96 registers) 157 ms
+// 32-bit index geometry of the two passes (the host rejects fields of 2^31
+// cells or more; their flux fields alone would exceed the device memory):
+// strides, the divisors of the cell and band coordinates, and the band
+// shape.  Band order of the spectral planes: bands of B values of m, l
+// outer inside a band, m inner, k fastest; B divides nm.  The CTAs that
+// run together then read the m +-1, +-2 neighbour planes of E (pass 1) and
+// the m-1 flux planes (pass 2) from L2 instead of HBM.
+struct FastGeom {
+  int s[6];                  // strides of the 6D fields
+  int ps[6][6];              // strides of the face-0 planes
+  unsigned nvol3, nspec;
+  DivU32 nx, ny;             // v3 -> x, y, z
+  DivU32 per_band, nk, B;    // u -> band, k, m in band, l
+};
+
+FastGeom make_geom(const Dims& d, int B) {
+  FastGeom G;
+  for (int a = 0; a < 6; a++) {
+    G.s[a] = (int)d.s[a];
+    for (int b = 0; b < 6; b++) G.ps[a][b] = (int)d.ps[a][b];
+  }
+  G.nvol3 = (unsigned)d.nvol3;
+  G.nspec = (unsigned)d.nspec;
+  G.nx = make_div((unsigned)d.n[0]);
+  G.ny = make_div((unsigned)d.n[1]);
+  G.per_band = make_div((unsigned)(d.n[3] * d.n[4] * B));
+  G.nk = make_div((unsigned)d.n[3]);
+  G.B = make_div((unsigned)B);
+  return G;
+}
+
+// coordinates of cell (v3, u) and its index: u is the plane's position in
+// band order
+__device__ __forceinline__ int cell_at(const Dims& d, const FastGeom& G, unsigned v3, unsigned u, int c[6]) {
+  const unsigned q = G.nx.div(v3);
+  c[0] = (int)(v3 - q * G.nx.d);
+  c[2] = (int)G.ny.div(q);
+  c[1] = (int)(q - (unsigned)c[2] * G.ny.d);
+  const unsigned b = G.per_band.div(u);
+  const unsigned r = u - b * G.per_band.d;
+  const unsigned r2 = G.nk.div(r);
+  c[3] = (int)(r - r2 * G.nk.d);
+  c[4] = (int)G.B.div(r2);
+  c[5] = (int)(b * G.B.d + (r2 - (unsigned)c[4] * G.B.d));
+  const unsigned sp = (unsigned)c[3] + (unsigned)d.n[3] * ((unsigned)c[4] + (unsigned)d.n[4] * (unsigned)c[5]);
+  return (int)(v3 + sp * G.nvol3);
+}
+
+// nb_index in 32-bit arithmetic
+__device__ __forceinline__ int nb32(const Dims& d, const FastGeom& G, int p, int a, int c, int off, int cm) {
+  int flip = 0;
+  const int c2 = map_coord(d, a, c + off, flip);
+  int q = p + (c2 - c) * G.s[a];
+  if (flip) q += ((d.n[5] - 1 - cm) - cm) * G.s[5];
+  return q;
+}
+
+__device__ __forceinline__ int plane32(const FastGeom& G, int a, const int c[6]) {
+  int q = 0;
+#pragma unroll
+  for (int b = 0; b < 6; b++) q += c[b] * G.ps[a][b];
+  return q;
+}
+
+// resident CTAs per SM the two passes are compiled for (register budgets
+// 40 and 32 per thread, no spills).  Both passes wait on scattered loads
+// of E and the flux fields, so warps in flight pay: at 32^6 the pair
+// measured 108.1 ms per step at 4/4 CTAs, 102.1 at 5/5, 98.8 at 6/6 and
+// 97.1 at 6/8 (the 64-bit index form at 4/4: 120.7 ms)
 #ifndef RT_FAST_MINB_FLUX
-#define RT_FAST_MINB_FLUX 4
+#define RT_FAST_MINB_FLUX 6
 #endif
 #ifndef RT_FAST_MINB_UPD
-#define RT_FAST_MINB_UPD 4
+#define RT_FAST_MINB_UPD 8
 #endif
 
 dim3 cells_grid(const Dims& d) {
   const long long bx = (d.nvol3 + 255) / 256;
   const long long by = d.nspec < 65535 ? d.nspec : 65535;
   return dim3((unsigned)bx, (unsigned)by, 1);
-}
-
-// The u-th spectral plane (k,l,m) in band order: bands of B values of m,
-// l outer inside a band, m inner, k fastest (B = 1: the natural order).
-// The CTAs that run together then read the m +-1, +-2 neighbour planes of E
-// (pass 1) and the m-1 flux planes (pass 2) from L2 instead of HBM.
-__device__ __forceinline__ long long band_plane(const Dims& d, long long u, int B) {
-  const int nk = d.n[3], nl = d.n[4], nm = d.n[5];
-  const long long per_band = (long long)nk * nl * B;
-  const long long b = u / per_band;
-  long long r = u - b * per_band;
-  const int bs = (b + 1) * B > nm ? nm - (int)b * B : B;   // the last band may be shorter
-  const int k = (int)(r % nk);
-  r /= nk;
-  const int m = (int)b * B + (int)(r % bs);
-  const int l = (int)(r / bs);
-  return k + (long long)nk * (l + (long long)nl * m);
 }
 
 // h = |v|/2 * (1 - |v*dt/d(f)|) of every face of axis a: right faces
@@ -118,31 +176,38 @@ __global__ void fast_mu_kernel(Dims d, Grid g, double dt, const double* lx, cons
   }
 }
 
-// pass 1: the right-face flux of every axis with n > 1 (and the face-0
-// flux at c_a = 0), one thread per cell
+// Face 0 of an axis whose lower boundary copies the edge cell (every axis
+// but z with the lower reflection): E(-2) = E(-1) = E(0), so Rj = 0, the
+// limited slope is 0 and the flux is v*E(0) exactly.  The update pass forms
+// it from the cell's own E (one multiply); only the reflected z face 0 (a
+// whole plane of cells) is evaluated in full by the flux pass.  Along x the
+// cells with c_x = 0 are one lane of every warp: a full flux evaluation
+// there would occupy the binary64 pipe for the whole warp's issue slots.
+__device__ __forceinline__ bool face0_is_copy(const Dims& d, int a) { return a != 2 || !d.lower_refl; }
+
+// pass 1: the right-face flux of every axis with n > 1 (and the reflected
+// z face 0), one thread per cell
 // ones: ~0 (see sel64)
 __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepArgs<double> A, SplitFluxes F,
-                                                                            int band, unsigned long long ones) {
+                                                                            FastGeom G, unsigned long long ones) {
   const Dims& d = A.d;
-  const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v3 >= d.nvol3) return;
-  for (long long u = blockIdx.y; u < d.nspec; u += gridDim.y) {
-    const long long sp = band_plane(d, u, band);
+  const unsigned v3 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v3 >= G.nvol3) return;
+  for (unsigned u = blockIdx.y; u < G.nspec; u += gridDim.y) {
     int c[6];
-    cell_coords(d, v3, sp, c);
-    const long long p = v3 + sp * d.nvol3;
+    const int p = cell_at(d, G, v3, u, c);
     const double e0 = A.E[p];
 #pragma unroll
     for (int a = 0; a < 6; a++) {
       if (d.n[a] <= 1) continue;
       const int ca = c[a];
-      const double Em1 = A.E[nb_index(d, p, a, ca, -1, c[5])];
-      const double Ep1 = A.E[nb_index(d, p, a, ca, +1, c[5])];
-      const double Ep2 = A.E[nb_index(d, p, a, ca, +2, c[5])];
+      const double Em1 = A.E[nb32(d, G, p, a, ca, -1, c[5])];
+      const double Ep1 = A.E[nb32(d, G, p, a, ca, +1, c[5])];
+      const double Ep2 = A.E[nb32(d, G, p, a, ca, +2, c[5])];
       __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2, ones));
-      if (ca == 0) {  // face 0: E(-2), E(-1), E(0), E(1) through the boundary maps
-        const long long q = plane_index(d, a, c);
-        const double Em2 = A.E[nb_index(d, p, a, ca, -2, c[5])];
+      if (ca == 0 && !face0_is_copy(d, a)) {  // E(-2), E(-1), E(0), E(1) through the boundary maps
+        const int q = plane32(G, a, c);
+        const double Em2 = A.E[nb32(d, G, p, a, ca, -2, c[5])];
         F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1, ones);
       }
     }
@@ -151,25 +216,30 @@ __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepA
 
 // pass 2: E_new = E*mu + sum_a c_a*(F_l - F_r), axis order x,y,z,k,l,m
 __global__ void __launch_bounds__(256, RT_FAST_MINB_UPD) fast_update_kernel(StepArgs<double> A, SplitFluxes F,
-                                                                            const double* mu, FastTab T, int band) {
+                                                                            const double* mu, FastTab T, FastGeom G) {
   const Dims& d = A.d;
-  const long long v3 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v3 >= d.nvol3) return;
-  for (long long u = blockIdx.y; u < d.nspec; u += gridDim.y) {
-    const long long sp = band_plane(d, u, band);
+  const unsigned v3 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v3 >= G.nvol3) return;
+  for (unsigned u = blockIdx.y; u < G.nspec; u += gridDim.y) {
     int c[6];
-    cell_coords(d, v3, sp, c);
-    const long long p = v3 + sp * d.nvol3;
+    const int p = cell_at(d, G, v3, u, c);
+    const double e0 = __ldcs(A.E + p);
     double acc = 0.0;
 #pragma unroll
     for (int a = 0; a < 6; a++) {
       if (d.n[a] <= 1) continue;
       const int ca = c[a];
       const double fr = F.f[a][p];   // also the left flux of cell p + s_a: kept in L2
-      const double fl = ca > 0 ? F.f[a][p - d.s[a]] : F.f0[a][plane_index(d, a, c)];
+      double fl;
+      if (ca > 0) {
+        fl = F.f[a][p - G.s[a]];
+      } else {
+        const int q = plane32(G, a, c);
+        fl = face0_is_copy(d, a) ? __dmul_rn(A.vlo[a][q], e0) : F.f0[a][q];
+      }
       acc = __fma_rn(T.c[a][pidx(ca + 1)], __dsub_rn(fl, fr), acc);
     }
-    __stcs(A.Enew + p, __fma_rn(__ldcs(A.E + p), __ldcs(mu + p), acc));
+    __stcs(A.Enew + p, __fma_rn(e0, __ldcs(mu + p), acc));
   }
 }
 
@@ -192,12 +262,17 @@ cudaError_t launch_fast_prepare(const Dims& d, const Grid& g, double dt, const d
 
 cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, const double* mu, const FastTab& T,
                              int band, cudaStream_t st) {
-  const dim3 g = cells_grid(A.d);
-  const int B = band < 1 ? 1 : (band > A.d.n[5] ? A.d.n[5] : band);
-  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, B, ~0ull);
+  const Dims& d = A.d;
+  if (d.ncell >= (1ll << 31)) return cudaErrorInvalidValue;
+  // the band: the largest divisor of nm not above the requested width
+  int B = band < 1 ? 1 : (band > d.n[5] ? d.n[5] : band);
+  while (d.n[5] % B) B--;
+  const FastGeom G = make_geom(d, B);
+  const dim3 g = cells_grid(d);
+  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, G, ~0ull);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, B);
+  fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, G);
   return cudaGetLastError();
 }
 

@@ -117,6 +117,23 @@ def test_fast_fp64_within_bound(name):
         m.close()
 
 
+@pytest.mark.parametrize("n", [(7, 3, 5, 2, 6, 10), (8, 8, 8, 4, 2, 6), (33, 2, 4, 2, 4, 8)])
+def test_fast_fp64_band_order_invariant(n):
+    """the band only orders the spectral planes among the CTAs (a width that
+    does not divide nm is reduced to one that does): every band gives the
+    same bits"""
+    exp = configs.shear_mini(n=n)
+    outs = []
+    for band in (1, 2, 3, 4, 8, 64):
+        m = configs.build_model(exp, "fp64")
+        m.set_tuning("fast", band, 256)
+        m.integrate(3)
+        outs.append(m.get_state()[interior(exp.n)].copy())
+        m.close()
+    for b, out in zip((2, 3, 4, 8, 64), outs[1:]):
+        assert np.array_equal(out, outs[0]), b
+
+
 def test_fast_fp64_switches_with_bit_exact_schedules():
     """switching between the fast and the bit-exact schedules on one handle
     (the per-face cache changes meaning between uCFL and h) keeps every
