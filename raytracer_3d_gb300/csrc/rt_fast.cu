@@ -187,9 +187,8 @@ __device__ __forceinline__ bool face0_is_copy(const Dims& d, int a) { return a !
 
 // pass 1: the right-face flux of every axis with n > 1 (and the reflected
 // z face 0), one thread per cell
-// ones: ~0 (see sel64)
 __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepArgs<double> A, SplitFluxes F,
-                                                                            FastGeom G, unsigned long long ones) {
+                                                                            FastGeom G) {
   const Dims& d = A.d;
   const unsigned v3 = blockIdx.x * blockDim.x + threadIdx.x;
   if (v3 >= G.nvol3) return;
@@ -204,11 +203,11 @@ __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepA
       const double Em1 = A.E[nb32(d, G, p, a, ca, -1, c[5])];
       const double Ep1 = A.E[nb32(d, G, p, a, ca, +1, c[5])];
       const double Ep2 = A.E[nb32(d, G, p, a, ca, +2, c[5])];
-      __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2, ones));
+      __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2));
       if (ca == 0 && !face0_is_copy(d, a)) {  // E(-2), E(-1), E(0), E(1) through the boundary maps
         const int q = plane32(G, a, c);
         const double Em2 = A.E[nb32(d, G, p, a, ca, -2, c[5])];
-        F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1, ones);
+        F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1);
       }
     }
   }
@@ -269,7 +268,7 @@ cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, co
   while (d.n[5] % B) B--;
   const FastGeom G = make_geom(d, B);
   const dim3 g = cells_grid(d);
-  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, G, ~0ull);
+  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, G);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, G);

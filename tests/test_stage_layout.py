@@ -66,3 +66,19 @@ def test_binary32_update_rounds_without_bias():
         print(r.stdout)
         assert r.returncode == 0, r.stdout + r.stderr
         assert " 0 failures" in r.stdout
+
+
+@pytest.mark.gpu
+def test_fast_superbee_selection_device_matches_host():
+    """the device form of the limiter (one block of integer PTX) gives the
+    host form's bits on every case of the host check"""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "superbee_select_check")
+        cmd = [_nvcc(), "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC,
+               os.path.join(HERE, "native", "superbee_select_check.cu"), "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        r = subprocess.run([out, "--device"], capture_output=True, text=True, timeout=300)
+        print(r.stdout)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert " 0 mismatches" in r.stdout
