@@ -222,20 +222,22 @@ FP32_CANDIDATES = ([(v, b, t, s) for v in ("w2z", "w2q", "w3", "w6") for t in (1
 FP64_CANDIDATES = [("tma", 8, 256, 0), ("split", 8, 256, 0), ("fast", 8, 256, 0)]
 
 
-def fp64_ops_per_cell(schedule, n):
+def fp64_ops_per_cell(schedule, n, lower_reflection=True):
     """binary64 pipe instructions (add, multiply, fma; each counted once) per
     cell-update of the fast schedule, from its source: per axis with n > 1,
-    4 per face flux (Rj, the upwind difference, v*E_up, the fma with h) on
-    n + 1 faces per n cells, and 2 in the update (F_l - F_r, the fma with
-    dt/d); plus the final fma with mu.  None for the bit-exact schedules,
-    whose divisions and comparisons are compiler sequences (their counts
-    come from ncu, profiles/)."""
+    4 per right-face flux (Rj, the upwind difference, v*E_up, the fma with
+    h) and 2 in the update (F_l - F_r, the fma with dt/d); the face-0 flux
+    of an axis, once per n cells, costs 1 (v*E(0), the edge copied into the
+    ghosts) or 4 (z with the lower reflection); plus the final fma with mu.
+    None for the bit-exact schedules, whose divisions and comparisons are
+    compiler sequences (their counts come from ncu, profiles/)."""
     if schedule != "fast":
         return None
     ops = 1.0
-    for k in n:
+    for a, k in enumerate(n):
         if k > 1:
-            ops += 4.0 * (1.0 + 1.0 / k) + 2.0
+            face0 = 4.0 if (a == 2 and lower_reflection) else 1.0
+            ops += 4.0 + 2.0 + face0 / k
     return ops
 
 
@@ -393,11 +395,13 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
         models.append(configs.build_model(e, "fp32", padded=False))   # no padded host array
     setup_s = time.perf_counter() - t0
     b = Batch(models)
-    if fixed:   # band, threads, sweep, persistent threads[, slice threads] (profiling runs)
+    if fixed:   # band, threads, sweep, persistent threads[, slice threads[, fused]] (profiling runs)
+        fixed = tuple(fixed) + (-1, 1)[len(fixed) - 4:]
         b.set_tuning(fixed[0], fixed[1], fixed[2], 16)
         b.set_persistent(fixed[3])
-        b.set_slices(fixed[4] if len(fixed) > 4 else -1)
-        best = tuple(fixed) + ((-1,) if len(fixed) < 5 else ())
+        b.set_slices(fixed[4])
+        b.set_fused(fixed[5])
+        best = fixed
     else:
         best, table = tune_batch(b, reps=2, use_cache=False)
     b.integrate(warmup)
@@ -415,11 +419,42 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
     b.sync()
     launches = b.launch_count() - l0
     cells = b.cells
+    # the fastest schedule that steps both warp-specialised classes in ONE
+    # launch, timed the same way when the tuner preferred another
+    one_launch = None
+    if not fixed:
+        fused = [c for c, _ in table if len(c) > 5 and c[5] == 1 and c[3] == c[4] and c[3] > 0]
+        if fused and tuple(fused[0]) != tuple(best):
+            c = fused[0]
+            b.set_tuning(c[0], c[1], c[2], 16)
+            b.set_persistent(c[3])
+            b.set_slices(c[4])
+            b.set_fused(1)
+            b.integrate(warmup)
+            b.sync()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            k0 = b.launch_count()
+            f0.record(stream)
+            b.integrate(steps)
+            f1.record(stream)
+            f1.synchronize()
+            fsecs = f0.elapsed_time(f1) / 1e3
+            one_launch = {"value": cells * steps / fsecs, "ms_per_step": 1e3 * fsecs / steps,
+                          "launches_per_step": (b.launch_count() - k0) / steps,
+                          "tuning": {"band": c[0], "threads": c[1], "sweep": c[2], "persistent_threads": c[3],
+                                     "slice_threads": c[4], "fused": True}}
+            b.set_tuning(best[0], best[1], best[2], 16)   # back to the timed schedule for the error run
+            b.set_persistent(best[3])
+            b.set_slices(best[4])
+            b.set_fused(best[5] if len(best) > 5 else 1)
+        elif fused:
+            one_launch = "the timed schedule"
     error = None
     if error_steps > 0:
         # every member on to error_steps in the batch, then each alone in
         # binary64 (the fast schedule) from the same initial state
-        taken = warmup + steps
+        taken = (warmup + steps) * (2 if isinstance(one_launch, dict) else 1)
         if error_steps > taken:
             b.integrate(error_steps - taken)
         b.sync()
@@ -448,9 +483,11 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
            "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": launches,
            "graph_steps": b.tuning[3],
            "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
-                      "slice_threads": best[4], "staged_members": b.persistent_members()},
+                      "slice_threads": best[4], "fused": bool(best[5]) if len(best) > 5 else True,
+                      "staged_members": b.persistent_members()},
+           "launches_per_step": launches / steps,
            "roofline": roofline("fp32", cells, secs / steps, "batch_fp32"), "clocks": cs.summary(),
-           "setup_s": round(setup_s, 2), "error": error}
+           "setup_s": round(setup_s, 2), "error": error, "one_launch_per_step": one_launch}
     b.close()
     for m in models:
         m.close()
@@ -658,7 +695,7 @@ def main():
     ap.add_argument("--batch-members", type=int, default=48)
     ap.add_argument("--batch-spatial", default=None, help="spatial extents of the members, e.g. 8,16 (profiling)")
     ap.add_argument("--batch-tuning", default=None,
-                    help="band,threads,sweep,persistent[,slices]: a fixed batch schedule instead of the batch tuner")
+                    help="band,threads,sweep,persistent[,slices[,fused]]: a fixed batch schedule instead of the batch tuner")
     ap.add_argument("--only", default="all", choices=("all", "batch", "serve"),
                     help="batch / serve: that form alone (profiling)")
     ap.add_argument("--serve-requests", type=int, default=60)

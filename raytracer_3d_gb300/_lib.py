@@ -88,6 +88,7 @@ SIGNATURES = {
     "rt_batch_set_persistent": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_batch_persistent_members": (ctypes.c_int, [_P]),
     "rt_batch_set_slices": (ctypes.c_int, [_P, ctypes.c_int]),
+    "rt_batch_set_fused": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_batch_integrate": (ctypes.c_int, [_P, ctypes.c_int]),
     "rt_batch_sync": (ctypes.c_int, [_P]),
     "rt_batch_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),

@@ -101,9 +101,10 @@ def tune_model(model, candidates=None, reps=3, use_cache=True):
 
 
 BATCH_CANDIDATES = [
-    (band, 512, sweep, persistent, slices)
+    (band, 512, sweep, persistent, slices, fused)
     for persistent in (256, 512, 0)
     for slices in (256, 512, 0)
+    for fused in ((1, 0) if persistent == slices and persistent > 0 else (1,))
     for band in (4, 8)
     for sweep in (0, 1)
 ]
@@ -111,16 +112,17 @@ BATCH_CANDIDATES = [
 
 def tune_batch(batch, candidates=None, reps=2, graph_steps=16, use_cache=True):
     """Pick band / CTA size / sweep order of the plane and group kernels and
-    the consumer threads of the two staged classes (0: off) for a Batch;
-    returns (best, table) with best = (band, threads, sweep, persistent,
-    slices)."""
-    key = signature("batch3", sorted(m.n for m in batch.models), batch.models[0].precision)
+    the consumer threads of the two staged classes (0: off) and whether
+    they share one launch for a Batch; returns (best, table) with best =
+    (band, threads, sweep, persistent, slices, fused)."""
+    key = signature("batch4", sorted(m.n for m in batch.models), batch.models[0].precision)
     cache = _load_cache() if use_cache else {}
 
     def apply(c):
         batch.set_tuning(c[0], c[1], c[2], graph_steps)
         batch.set_persistent(c[3])
         batch.set_slices(c[4])
+        batch.set_fused(c[5] if len(c) > 5 else 1)
 
     if use_cache and key in cache:
         apply(cache[key]["best"])

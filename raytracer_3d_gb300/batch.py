@@ -27,6 +27,8 @@ class Batch:
             m._state_on_device = True
         self.tuning = (8, 256, 0, 16)
         self.persistent = 256
+        self.slices = -1
+        self.fused = True
 
     def _check(self, rc, what):
         if rc != 0:
@@ -45,6 +47,12 @@ class Batch:
         """consumer threads of the small-plane class (0: off, -1: as set_persistent)"""
         self._check(self._lib.rt_batch_set_slices(self._b, int(threads)), "rt_batch_set_slices")
         self.slices = int(threads)
+
+    def set_fused(self, on=True):
+        """one launch per step for both warp-specialised classes (default)
+        or one launch per class"""
+        self._check(self._lib.rt_batch_set_fused(self._b, int(bool(on))), "rt_batch_set_fused")
+        self.fused = bool(on)
 
     def persistent_members(self):
         n = self._lib.rt_batch_persistent_members(self._b)

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libraytracer_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["rt_api.cu", "rt_kernels.cu", "rt_persist.cu", "rt_persist_w2.cu", "rt_noalloc.cu",
+SOURCES = ["rt_api.cu", "rt_kernels.cu", "rt_persist.cu", "rt_persist_w2.cu", "rt_persist_fused.cu", "rt_noalloc.cu",
            "rt_forcing.cu", "rt_split.cu", "rt_fast.cu", "rt_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",

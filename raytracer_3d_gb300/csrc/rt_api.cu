@@ -395,6 +395,11 @@ struct rt_batch {
   int sns = 0, sgrid = 0, sthreads = 0;
   long long sstage = 0;
   int slice_threads = -1;       // consumer threads of the z-slice class; -1: as pthreads, 0: off
+  long long pcells = 0, scells = 0;   // cells of the two persistent classes
+  // both persistent classes in one launch (batch_fused_kernel) when they
+  // share a thread count: grid and the CTAs of the fully staged class
+  int fuse = 1;                 // setting (rt_batch_set_fused)
+  int fgrid = 0, fga = 0;       // 0: two launches
 };
 
 static int bfail(rt_batch* b, int code, const char* fmt, ...) {
@@ -422,7 +427,86 @@ static void batch_free_graphs(rt_batch* b) {
 
 // kernel launches per batch step
 static int batch_kernels(const rt_batch* b) {
-  return (int)b->forced.size() + (b->np > 0 ? 1 : 0) + (b->ns6 > 0 ? 1 : 0) + (b->nq > 0 ? 1 : 0);
+  const int persistent = b->fgrid > 0 ? 1 : (b->np > 0 ? 1 : 0) + (b->ns6 > 0 ? 1 : 0);
+  return (int)b->forced.size() + persistent + (b->nq > 0 ? 1 : 0);
+}
+
+static BatchFused batch_fused_args(const rt_batch* b, int par) {
+  BatchFused F;
+  F.pmem = b->d_pmem[par];
+  F.pfirst = b->d_pfirst;
+  F.np = b->np;
+  F.pR = b->pR;
+  F.pns = b->pns;
+  F.pstage = b->pstage;
+  F.smem6 = b->d_smem6[par];
+  F.sfirst = b->d_sfirst;
+  F.ns6 = b->ns6;
+  F.sns = b->sns;
+  F.sstage = b->sstage;
+  F.threads = b->pthreads;
+  return F;
+}
+
+// device time of one class's own launch (0: fully staged, 1: small
+// planes) from the members' current states into the other buffers, the
+// way a dry step runs (nothing advances); the second of two launches, in
+// ms, or a negative value when a launch or an event fails
+static float batch_class_ms(rt_batch* b, int cls) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return -1.f;
+  }
+  cudaError_t e = cudaSuccess;
+  for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {
+    cudaEventRecord(e0, b->st);
+    e = cls == 0 ? launch_batch_w3(b->d_pmem[0], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage,
+                                   b->pgrid, b->st)
+                 : launch_batch_w6(b->d_smem6[0], b->d_sfirst, b->ns6, b->sthreads, b->sns, b->sstage, b->sgrid,
+                                   b->st);
+    cudaEventRecord(e1, b->st);
+  }
+  float ms = -1.f;
+  if (e == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+    ms = -1.f;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+// one launch for both persistent classes when they run the same thread
+// count: the grid of the fused kernel, split between the classes in
+// proportion to the device time of each class's own launch (so both
+// shares finish together; by their cells if the timing fails), at least
+// one CTA each; fgrid = 0 otherwise
+static void batch_plan_fused(rt_batch* b) {
+  b->fgrid = b->fga = 0;
+  if (!b->fuse || b->np == 0 || b->ns6 == 0 || b->sthreads != b->pthreads) return;
+  const int per_sm = batch_fused_blocks_per_sm(batch_fused_args(b, 0));
+  if (per_sm < 1) return;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = per_sm * nsm;
+  if (grid < 2) return;
+  double share = (double)b->pcells / (double)(b->pcells + b->scells);
+  // the timing launches write the members' other buffers: ordered after
+  // everything queued on the members' streams, and before what follows
+  bool ordered = true;
+  for (rt_handle* h : b->mem)
+    ordered = ordered && cudaEventRecord(h->ev, h->st) == cudaSuccess &&
+              cudaStreamWaitEvent(b->st, h->ev, 0) == cudaSuccess;
+  if (ordered) {
+    const float ta = batch_class_ms(b, 0), tb = batch_class_ms(b, 1);
+    if (ta > 0.f && tb > 0.f) share = ta / (double)(ta + tb);
+    if (cudaEventRecord(b->ev, b->st) == cudaSuccess)
+      for (rt_handle* h : b->mem) cudaStreamWaitEvent(h->st, b->ev, 0);
+  }
+  int ga = (int)(share * grid + 0.5);
+  ga = std::max(1, std::min(grid - 1, ga));
+  b->fgrid = grid;
+  b->fga = ga;
 }
 
 // one step of every member, starting from the arrays of parity `par`;
@@ -436,10 +520,15 @@ static cudaError_t batch_launch(rt_batch* b, int par, bool force = true) {
       e = apply_forcing(b->mem[j], b->cur0[j] ^ par, b->st);
       if (e != cudaSuccess) return e;
     }
-  if (b->np)
-    e = launch_batch_w3(b->d_pmem[par], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage, b->pgrid, b->st);
-  if (e == cudaSuccess && b->ns6)
-    e = launch_batch_w6(b->d_smem6[par], b->d_sfirst, b->ns6, b->sthreads, b->sns, b->sstage, b->sgrid, b->st);
+  if (b->fgrid > 0) {
+    e = launch_batch_fused(batch_fused_args(b, par), b->fgrid, b->fga, b->st);
+  } else {
+    if (b->np)
+      e = launch_batch_w3(b->d_pmem[par], b->d_pfirst, b->np, b->pthreads, b->pR, b->pns, b->pstage, b->pgrid,
+                          b->st);
+    if (e == cudaSuccess && b->ns6)
+      e = launch_batch_w6(b->d_smem6[par], b->d_sfirst, b->ns6, b->sthreads, b->sns, b->sstage, b->sgrid, b->st);
+  }
   if (e != cudaSuccess || !b->nq) return e;
   const void* mem = b->d_mem[par];
   const int n = b->nq;
@@ -506,6 +595,8 @@ static int batch_build_persistent(rt_batch* b, std::vector<int>& rest) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   b->pgrid = (int)std::min<long long>(first.back(), (long long)per_sm * nsm);
   b->np = (int)pm.size();
+  b->pcells = 0;
+  for (int j : pm) b->pcells += b->mem[j]->d.ncell;
   return RT_OK;
 }
 
@@ -563,6 +654,8 @@ static int batch_build_slices(rt_batch* b, std::vector<int>& rest) {
   b->sstage = stage;
   b->sthreads = nt;
   b->ns6 = (int)sm.size();
+  b->scells = 0;
+  for (int j : sm) b->scells += b->mem[j]->d.ncell;
   rest = left;
   return RT_OK;
 }
@@ -574,6 +667,7 @@ static int batch_build(rt_batch* b) {
   if (rc) return rc;
   rc = batch_build_slices<T>(b, qm);
   if (rc) return rc;
+  batch_plan_fused(b);
   const int n = (int)qm.size();
   b->nq = n;
   std::vector<BatchMember<T>> arr[2];
@@ -795,6 +889,14 @@ int rt_batch_set_slices(rt_batch* b, int threads) {
   return RT_OK;
 }
 
+int rt_batch_set_fused(rt_batch* b, int on) {
+  if (!b) return RT_ERR_ARG;
+  if (on != 0 && on != 1) return bfail(b, RT_ERR_ARG, "rt_batch_set_fused: on must be 0 or 1");
+  cudaStreamSynchronize(b->st);
+  b->fuse = on;
+  b->dirty = true;
+  return RT_OK;
+}
 int rt_batch_persistent_members(rt_batch* b) {
   if (!b) return RT_ERR_ARG;
   if (b->dirty) {

@@ -133,6 +133,23 @@ size_t w6_smem(int ns, long long stage_floats);
 int w6_blocks_per_sm(int threads, size_t smem);
 cudaError_t launch_batch_w6(const void* members, const long long* first, int nmem, int threads, int ns,
                             long long stage_floats, int grid, cudaStream_t st);
+// both binary32 ensemble classes in one launch (rt_persist_fused.cu):
+// the arguments of the two launches above, one thread count for both, the
+// grid and the CTAs [0, ga) of the fully staged class
+struct BatchFused {
+  const void* pmem;
+  const long long* pfirst;
+  int np, pR, pns;
+  long long pstage;
+  const void* smem6;
+  const long long* sfirst;
+  int ns6, sns;
+  long long sstage;
+  int threads;
+};
+size_t batch_fused_smem(const BatchFused& F);
+int batch_fused_blocks_per_sm(const BatchFused& F);
+cudaError_t launch_batch_fused(const BatchFused& F, int grid, int ga, cudaStream_t st);
 // persistent binary32 kernels (dispatch in rt_persist.cu; the families in
 // rt_persist.cu, rt_persist_w2.cu); done = false when the tuning
 // does not select one of them or the shape does not fit them

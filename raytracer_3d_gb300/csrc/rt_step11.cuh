@@ -415,10 +415,14 @@ __device__ __forceinline__ void w6_item(const StepArgs<float>& A, const W6Geom& 
 // one field (mem == nullptr: A, S, nitems) or the members of an ensemble
 // (member j owns items [first[j], first[j+1]), its slices per item in
 // mem[j].S.gz; nitems = first[nmem])
+// The CTA's part as a device function: bid / nb stand for the block index
+// and the grid size (batch_fused_kernel gives a share of its CTAs to this
+// class).
 template <int NT>
-__global__ void __launch_bounds__(NT + 32, 1)
-    step_w6_kernel(StepArgs<float> A, PlaneSched S, const BatchMember<float>* __restrict__ mem,
-                   const long long* __restrict__ first, int nmem, long long nitems, int ns, long long stage_floats) {
+__device__ __forceinline__ void step_w6_cta(const StepArgs<float>& A, const PlaneSched& S,
+                                            const BatchMember<float>* __restrict__ mem,
+                                            const long long* __restrict__ first, int nmem, long long nitems, int ns,
+                                            long long stage_floats, long long bid, long long nb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
   uint64_t* empty = full + RT_WS_MAXSTAGE;
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
     fence_mbar_init();
   }
   __syncthreads();
-  if (blockIdx.x >= nitems) return;
+  if (bid >= nitems) return;
 
   if (threadIdx.x >= NT) {
     int s = 0, j = 0, jcached = -1;
@@ -446,7 +450,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
         reinterpret_cast<BatchMember<float>*>(smem_raw + 128 + RT_WS_MAXSTAGE * w6_desc_bytes());
     uint32_t rnd = 0;
     long long issued = 0;
-    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    for (long long it = bid; it < nitems; it += nb) {
       if (mem) {
         while (it >= first_next) {
           j++;
@@ -479,7 +483,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
   int jc = -1;
   int s = 0;
   uint32_t par = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+  for (long long it = bid; it < nitems; it += nb) {
     if (!ws_wait(&dful[s], par, status)) return;
     const int j = desc[s].member;
     const StepArgs<float>& Aj = mem ? mem[j].A : A;
@@ -492,6 +496,38 @@ __global__ void __launch_bounds__(NT + 32, 1)
     w6_item(Aj, w, desc[s], stage0 + (size_t)s * stage_floats, lane);
     mbar_arrive(&empty[s]);
     if (++s == ns) { s = 0; par ^= 1u; }
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT + 32, 1)
+    step_w6_kernel(StepArgs<float> A, PlaneSched S, const BatchMember<float>* __restrict__ mem,
+                   const long long* __restrict__ first, int nmem, long long nitems, int ns, long long stage_floats) {
+  step_w6_cta<NT>(A, S, mem, first, nmem, nitems, ns, stage_floats, blockIdx.x, gridDim.x);
+}
+
+}  // namespace rt
+
+namespace rt {
+
+// One launch for a whole batched step of the binary32 ensemble: CTAs
+// [0, ga) step the members of the fully staged class (batch_w3_cta, planes
+// that fill a CTA), the others the members of the small-plane class
+// (step_w6_cta).  The host sizes ga in proportion to the two classes'
+// cells (both classes run at about the same cost per cell), so both shares
+// of the grid finish together; each CTA keeps one role for the launch, so
+// the roles' barriers and shared-memory layouts never mix.
+template <int NT, int R>
+__global__ void __launch_bounds__(NT + 32, 1)
+    batch_fused_kernel(const BatchMember<float>* __restrict__ pmem, const long long* __restrict__ pfirst, int np,
+                       int pns, long long pstage, const BatchMember<float>* __restrict__ smem6,
+                       const long long* __restrict__ sfirst, int ns6, int sns, long long sstage, int ga,
+                       StepArgs<float> none, PlaneSched no_sched) {   // unused: the members carry their arguments
+  if ((int)blockIdx.x < ga) {
+    batch_w3_cta<NT, R>(pmem, pfirst, np, pns, pstage, blockIdx.x, ga);
+  } else {
+    step_w6_cta<NT>(none, no_sched, smem6, sfirst, ns6, -1, sns, sstage, (long long)blockIdx.x - ga,
+                    (long long)gridDim.x - ga);
   }
 }
 

@@ -408,10 +408,13 @@ __global__ void __launch_bounds__(NT + 32, 1) step_w3_kernel(StepArgs<float> A, 
 // items [first[j], first[j+1]) of its own band order), walked by persistent
 // CTAs; stages are sized for the largest member plane (stage_floats).  The
 // consumers recompute their block geometry when the member changes.
+// The CTA's part as a device function: bid / nb stand for the block index
+// and the grid size, so a kernel can give a share of its CTAs to this class
+// (batch_fused_kernel, rt_step11.cuh).
 template <int NT, int R>
-__global__ void __launch_bounds__(NT + 32, 1)
-    batch_w3_kernel(const BatchMember<float>* __restrict__ mem, const long long* __restrict__ first, int nmem,
-                    int ns, long long stage_floats) {
+__device__ __forceinline__ void batch_w3_cta(const BatchMember<float>* __restrict__ mem,
+                                             const long long* __restrict__ first, int nmem, int ns,
+                                             long long stage_floats, long long bid, long long nb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
   uint64_t* empty = full + RT_WS_MAXSTAGE;
@@ -430,13 +433,13 @@ __global__ void __launch_bounds__(NT + 32, 1)
     fence_mbar_init();
   }
   __syncthreads();
-  if (blockIdx.x >= nitems) return;
+  if (bid >= nitems) return;
 
   if (threadIdx.x >= NT) {
     int s = 0, j = 0;
     uint32_t rnd = 0;
     long long issued = 0;
-    for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+    for (long long it = bid; it < nitems; it += nb) {
       while (it >= first[j + 1]) j++;
       const W3Prep P = w3_prepare(mem[j].A, mem[j].S, it - first[j], stage0 + (size_t)s * stage_floats);
       if (rnd > 0 && !warp_wait(&empty[s], (rnd - 1) & 1u, status)) break;
@@ -453,7 +456,7 @@ __global__ void __launch_bounds__(NT + 32, 1)
   int jc = -1;
   int s = 0;
   uint32_t par = 0;
-  for (long long it = blockIdx.x; it < nitems; it += gridDim.x) {
+  for (long long it = bid; it < nitems; it += nb) {
     if (!ws_wait(&dful[s], par, status)) return;
     const int j = desc[s].member;
     const StepArgs<float>& A = mem[j].A;
@@ -467,6 +470,13 @@ __global__ void __launch_bounds__(NT + 32, 1)
     mbar_arrive(&empty[s]);
     if (++s == ns) { s = 0; par ^= 1u; }
   }
+}
+
+template <int NT, int R>
+__global__ void __launch_bounds__(NT + 32, 1)
+    batch_w3_kernel(const BatchMember<float>* __restrict__ mem, const long long* __restrict__ first, int nmem,
+                    int ns, long long stage_floats) {
+  batch_w3_cta<NT, R>(mem, first, nmem, ns, stage_floats, blockIdx.x, gridDim.x);
 }
 
 }  // namespace rt

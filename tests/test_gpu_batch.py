@@ -106,3 +106,36 @@ def test_mixed_classes_equal_members_alone(persistent):
     b.close()
     for m in models:
         m.close()
+
+
+@pytest.mark.parametrize("threads", [256, 512])
+def test_fused_launch_equals_two_launches_and_alone(threads):
+    """members of both warp-specialised classes (planes that fill the CTA,
+    small planes in z slices) stepped by ONE launch per step give each
+    member exactly its result alone, as the two launches per step do"""
+    from raytracer_3d_gb300.batch import Batch
+    dims = [(32, 16, 4, 4, 2, 4), (32, 32, 4, 2, 2, 4), (8, 8, 8, 4, 4, 2), (8, 8, 8, 2, 4, 4), (16, 8, 4, 2, 2, 2)]
+    exps = [configs.shear_mini(n=n, seed=40 + i) for i, n in enumerate(dims)]
+    alone = []
+    for e in exps:
+        m = configs.build_model(e, "fp32")
+        m.integrate(5)
+        alone.append(m.get_state().copy())
+        m.close()
+    for fused in (True, False):
+        models = [configs.build_model(e, "fp32") for e in exps]
+        b = Batch(models)
+        b.set_tuning(4, 256, 0, 2)
+        b.set_persistent(threads)
+        b.set_fused(fused)
+        assert b.persistent_members() == len(exps)
+        l0 = b.launch_count()
+        b.integrate(2)
+        b.integrate(3)          # graphs and a single launch, both parities
+        assert b.launch_count() - l0 == (5 if fused else 10), fused
+        for e, m, ref in zip(exps, models, alone):
+            sl = interior(e.n)
+            assert np.array_equal(m.get_state()[sl], ref[sl]), (fused, e.n)
+        b.close()
+        for m in models:
+            m.close()
