@@ -226,18 +226,21 @@ def fp64_ops_per_cell(schedule, n, lower_reflection=True):
     """binary64 pipe instructions (add, multiply, fma; each counted once) per
     cell-update of the fast schedule, from its source: per axis with n > 1,
     4 per right-face flux (Rj, the upwind difference, v*E_up, the fma with
-    h) and 2 in the update (F_l - F_r, the fma with dt/d); the face-0 flux
-    of an axis, once per n cells, costs 1 (v*E(0), the edge copied into the
-    ghosts) or 4 (z with the lower reflection); plus the final fma with mu.
-    None for the bit-exact schedules, whose divisions and comparisons are
-    compiler sequences (their counts come from ncu, profiles/)."""
+    h; 3 along x when nx divides 32, where the lanes of a row share their
+    differences) and 2 in the update (F_l - F_r, the fma with dt/d); the
+    face-0 flux of an axis, once per n cells, costs 1 (v*E(0), the edge
+    copied into the ghosts) or 4 (z with the lower reflection); plus the
+    final fma with mu.  None for the bit-exact schedules, whose divisions
+    and comparisons are compiler sequences (their counts come from ncu,
+    profiles/)."""
     if schedule != "fast":
         return None
     ops = 1.0
     for a, k in enumerate(n):
         if k > 1:
             face0 = 4.0 if (a == 2 and lower_reflection) else 1.0
-            ops += 4.0 + 2.0 + face0 / k
+            flux = 3.0 if (a == 0 and 32 % k == 0) else 4.0
+            ops += flux + 2.0 + face0 / k
     return ops
 
 
@@ -396,7 +399,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
     setup_s = time.perf_counter() - t0
     b = Batch(models)
     if fixed:   # band, threads, sweep, persistent threads[, slice threads[, fused]] (profiling runs)
-        fixed = tuple(fixed) + (-1, 1)[len(fixed) - 4:]
+        fixed = tuple(fixed) + (-1, 0)[len(fixed) - 4:]
         b.set_tuning(fixed[0], fixed[1], fixed[2], 16)
         b.set_persistent(fixed[3])
         b.set_slices(fixed[4])
@@ -447,7 +450,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
             b.set_tuning(best[0], best[1], best[2], 16)   # back to the timed schedule for the error run
             b.set_persistent(best[3])
             b.set_slices(best[4])
-            b.set_fused(best[5] if len(best) > 5 else 1)
+            b.set_fused(best[5] if len(best) > 5 else 0)
         elif fused:
             one_launch = "the timed schedule"
     error = None
@@ -483,7 +486,7 @@ def bench_batched(steps, warmup, members=48, seed=2024, fixed=None, spatial=None
            "steps": steps, "ms_per_step": 1e3 * secs / steps, "launches": launches,
            "graph_steps": b.tuning[3],
            "tuning": {"band": best[0], "threads": best[1], "sweep": best[2], "persistent_threads": best[3],
-                      "slice_threads": best[4], "fused": bool(best[5]) if len(best) > 5 else True,
+                      "slice_threads": best[4], "fused": bool(best[5]) if len(best) > 5 else False,
                       "staged_members": b.persistent_members()},
            "launches_per_step": launches / steps,
            "roofline": roofline("fp32", cells, secs / steps, "batch_fp32"), "clocks": cs.summary(),

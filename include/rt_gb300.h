@@ -272,10 +272,12 @@ int rt_batch_set_persistent(rt_batch* b, int threads);
 /* consumer threads (256 or 512) of the small-plane class alone; 0 turns
  * that class off, -1 (default) follows rt_batch_set_persistent */
 int rt_batch_set_slices(rt_batch* b, int threads);
-/* 1 (default): when both warp-specialised classes have members and run the
- * same consumer thread count, a batched step is ONE persistent launch whose
- * CTAs are split between the classes in proportion to their cells;
- * 0: one launch per class.  No effect on results. */
+/* 1: when both warp-specialised classes have members and run the same
+ * consumer thread count, a batched step is ONE persistent launch whose CTAs
+ * are split between the classes in proportion to the device time of each
+ * class's own launch, measured when the batch is (re)built -- a build then
+ * waits for the work queued before it; 0 (default): one launch per class.
+ * No effect on results. */
 int rt_batch_set_fused(rt_batch* b, int on);
 /* number of members in the two warp-specialised classes (negative: error) */
 int rt_batch_persistent_members(rt_batch* b);

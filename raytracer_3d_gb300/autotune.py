@@ -122,7 +122,7 @@ def tune_batch(batch, candidates=None, reps=2, graph_steps=16, use_cache=True):
         batch.set_tuning(c[0], c[1], c[2], graph_steps)
         batch.set_persistent(c[3])
         batch.set_slices(c[4])
-        batch.set_fused(c[5] if len(c) > 5 else 1)
+        batch.set_fused(c[5] if len(c) > 5 else 0)
 
     if use_cache and key in cache:
         apply(cache[key]["best"])

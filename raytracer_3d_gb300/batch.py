@@ -28,7 +28,7 @@ class Batch:
         self.tuning = (8, 256, 0, 16)
         self.persistent = 256
         self.slices = -1
-        self.fused = True
+        self.fused = False
 
     def _check(self, rc, what):
         if rc != 0:
@@ -49,8 +49,10 @@ class Batch:
         self.slices = int(threads)
 
     def set_fused(self, on=True):
-        """one launch per step for both warp-specialised classes (default)
-        or one launch per class"""
+        """one launch per step for both warp-specialised classes, or one
+        launch per class (the default).  The one-launch form times each
+        class's launch when the batch is rebuilt, which waits for the work
+        queued before the rebuild."""
         self._check(self._lib.rt_batch_set_fused(self._b, int(bool(on))), "rt_batch_set_fused")
         self.fused = bool(on)
 

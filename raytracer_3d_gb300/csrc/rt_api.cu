@@ -398,7 +398,7 @@ struct rt_batch {
   long long pcells = 0, scells = 0;   // cells of the two persistent classes
   // both persistent classes in one launch (batch_fused_kernel) when they
   // share a thread count: grid and the CTAs of the fully staged class
-  int fuse = 1;                 // setting (rt_batch_set_fused)
+  int fuse = 0;                 // setting (rt_batch_set_fused)
   int fgrid = 0, fga = 0;       // 0: two launches
 };
 

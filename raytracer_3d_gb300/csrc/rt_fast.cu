@@ -186,12 +186,26 @@ __global__ void fast_mu_kernel(Dims d, Grid g, double dt, const double* lx, cons
 __device__ __forceinline__ bool face0_is_copy(const Dims& d, int a) { return a != 2 || !d.lower_refl; }
 
 // pass 1: the right-face flux of every axis with n > 1 (and the reflected
-// z face 0), one thread per cell
+// z face 0), one thread per cell.
+// XW: x rows are whole segments of a warp (nx divides 32; CTAs of 256
+// threads start on a row).  The x faces then share their differences:
+// lane x forms D(x) = E(x+1) - E(x) once, the upwind difference of face
+// x+1/2 is D(x-1) or D(x+1) from the neighbouring lane, and E(x+1) comes
+// from the next lane too -- one binary64 subtraction per x face instead of
+// two, and no x-neighbour loads.  The operands and operations are those of
+// flux_fast64, so the fluxes are the same bits; beyond the row ends the
+// ghost cells copy the edge, so D(-1) = D(nx-1) = D(nx) = 0 there.  Lanes
+// past the last cell run on a clamped cell (the shuffles need every lane)
+// and store nothing.
+template <bool XW>
 __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepArgs<double> A, SplitFluxes F,
                                                                             FastGeom G) {
   const Dims& d = A.d;
-  const unsigned v3 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v3 >= G.nvol3) return;
+  const unsigned v3raw = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = v3raw < G.nvol3;
+  if (!XW && !valid) return;
+  const unsigned v3 = valid ? v3raw : G.nvol3 - 1;
+  const int nx = d.n[0];
   for (unsigned u = blockIdx.y; u < G.nspec; u += gridDim.y) {
     int c[6];
     const int p = cell_at(d, G, v3, u, c);
@@ -200,11 +214,24 @@ __global__ void __launch_bounds__(256, RT_FAST_MINB_FLUX) fast_flux_kernel(StepA
     for (int a = 0; a < 6; a++) {
       if (d.n[a] <= 1) continue;
       const int ca = c[a];
+      if (XW && a == 0) {
+        const double Ep1 = __shfl_down_sync(0xffffffffu, e0, 1, nx);   // the row's last lane: its own E
+        const double Rj = __dsub_rn(Ep1, e0);
+        const double Dm = __shfl_up_sync(0xffffffffu, Rj, 1, nx);
+        const double Dp = __shfl_down_sync(0xffffffffu, Rj, 1, nx);
+        const double v = __ldcs(A.vel[0] + p), h = __ldcs(A.uc[0] + p);
+        const bool pos = f64_pos(v);
+        const double up = pos ? (ca > 0 ? Dm : 0.0) : (ca < nx - 1 ? Dp : 0.0);
+        const double Fx = __fma_rn(h, superbee_slope64(Rj, up), __dmul_rn(v, pos ? e0 : Ep1));
+        if (valid) __stcs(F.f[0] + p, Fx);
+        continue;
+      }
       const double Em1 = A.E[nb32(d, G, p, a, ca, -1, c[5])];
       const double Ep1 = A.E[nb32(d, G, p, a, ca, +1, c[5])];
       const double Ep2 = A.E[nb32(d, G, p, a, ca, +2, c[5])];
-      __stcs(F.f[a] + p, flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2));
-      if (ca == 0 && !face0_is_copy(d, a)) {  // E(-2), E(-1), E(0), E(1) through the boundary maps
+      const double Fa = flux_fast64(__ldcs(A.vel[a] + p), __ldcs(A.uc[a] + p), Em1, e0, Ep1, Ep2);
+      if (valid) __stcs(F.f[a] + p, Fa);
+      if (valid && ca == 0 && !face0_is_copy(d, a)) {  // E(-2), E(-1), E(0), E(1) through the boundary maps
         const int q = plane32(G, a, c);
         const double Em2 = A.E[nb32(d, G, p, a, ca, -2, c[5])];
         F.f0[a][q] = flux_fast64(A.vlo[a][q], A.ucl[a][q], Em2, Em1, e0, Ep1);
@@ -268,7 +295,8 @@ cudaError_t launch_step_fast(const StepArgs<double>& A, const SplitFluxes& F, co
   while (d.n[5] % B) B--;
   const FastGeom G = make_geom(d, B);
   const dim3 g = cells_grid(d);
-  fast_flux_kernel<<<g, 256, 0, st>>>(A, F, G);
+  if (d.n[0] >= 2 && 32 % d.n[0] == 0) fast_flux_kernel<true><<<g, 256, 0, st>>>(A, F, G);
+  else fast_flux_kernel<false><<<g, 256, 0, st>>>(A, F, G);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   fast_update_kernel<<<g, 256, 0, st>>>(A, F, mu, T, G);

@@ -515,38 +515,11 @@ cudaError_t launch_max_rate(const Dims& d, const Grid& g, const ConstCoeff64& cf
 
 // ---- padded host array <-> unpadded device field, read / written by the GPU
 // through the host's page tables (devices with pageable memory access) ----
-// Row r of the interior is (y, z, k, l, m) in x-fastest order; the host
-// array is padded by RT_ONX on every axis (Fortran order).  The transfer
-// is bound by the latency of the CPU-GPU link, so every warp keeps
-// several rows in flight: with nx even and the host array 16-byte aligned
-// a lane moves a pair of values, nx/2 lanes a row, and a warp takes
-// 32/(nx/2) rows per pass (RT_HOST_ROWS passes unrolled); otherwise one
-// value per lane and a row per warp pass.
-#ifndef RT_HOST_ROWS
-#define RT_HOST_ROWS 4
-#endif
-#ifndef RT_HOST_BLOCKS
-#define RT_HOST_BLOCKS (16 * 152)
-#endif
-
-__device__ __forceinline__ long long host_row_offset(const Dims& d, const long long P[6], long long r) {
-  long long q = r;
-  const int j = (int)(q % d.n[1]); q /= d.n[1];
-  const int k = (int)(q % d.n[2]); q /= d.n[2];
-  const int l = (int)(q % d.n[3]); q /= d.n[3];
-  const int n = (int)(q % d.n[4]);
-  const int m = (int)(q / d.n[4]);
-  return RT_ONX + P[0] * ((j + RT_ONX) + P[1] * ((k + RT_ONX) + P[2] *
-         ((l + RT_ONX) + P[3] * ((n + RT_ONX) + P[4] * (long long)(m + RT_ONX)))));
-}
-
-template <class T> struct Pair;
-template <> struct Pair<double> { using type = double2; };
-template <> struct Pair<float> { using type = float2; };
-
+// A warp moves one x row: row r of the interior is (y, z, k, l, m) in x-fastest
+// order; the host array is padded by RT_ONX on every axis (Fortran order).
 template <bool TO_DEVICE, class T>
 __global__ void host_rows_kernel(const double* __restrict__ hsrc, double* __restrict__ hdst,
-                                 const T* __restrict__ dsrc, T* __restrict__ ddst, Dims d, int paired) {
+                                 const T* __restrict__ dsrc, T* __restrict__ ddst, Dims d) {
   long long P[6];
 #pragma unroll
   for (int a = 0; a < 6; a++) P[a] = d.n[a] + 2 * RT_ONX;
@@ -554,71 +527,31 @@ __global__ void host_rows_kernel(const double* __restrict__ hsrc, double* __rest
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
-  const int nx = d.n[0];
-  if (paired) {
-    using T2 = typename Pair<T>::type;
-    const int hx = nx >> 1;                 // lanes per row
-    const int rpw = 32 / hx;                // rows per warp pass
-    const int sub = lane / hx, x2 = lane - sub * hx;
-    const bool active = sub < rpw;
-    const long long step = nwarp * rpw;
-    for (long long r0 = warp * rpw; r0 < rows; r0 += step * RT_HOST_ROWS) {
-      double2 hv[RT_HOST_ROWS];
-      T2 dv[RT_HOST_ROWS];
-      long long hoff[RT_HOST_ROWS], doff[RT_HOST_ROWS];
-      bool ok[RT_HOST_ROWS];
-#pragma unroll
-      for (int u = 0; u < RT_HOST_ROWS; u++) {
-        const long long r = r0 + u * step + sub;
-        ok[u] = active && r < rows;
-        hoff[u] = ok[u] ? host_row_offset(d, P, r) + 2 * x2 : 0;
-        doff[u] = r * nx + 2 * x2;
-        if (TO_DEVICE) {
-          if (ok[u]) hv[u] = *reinterpret_cast<const double2*>(hsrc + hoff[u]);
-        } else {
-          if (ok[u]) dv[u] = *reinterpret_cast<const T2*>(dsrc + doff[u]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < RT_HOST_ROWS; u++) {
-        if (!ok[u]) continue;
-        if (TO_DEVICE) {
-          T2 v;
-          v.x = (T)hv[u].x;
-          v.y = (T)hv[u].y;
-          *reinterpret_cast<T2*>(ddst + doff[u]) = v;
-        } else {
-          *reinterpret_cast<double2*>(hdst + hoff[u]) = make_double2((double)dv[u].x, (double)dv[u].y);
-        }
-      }
-    }
-    return;
-  }
   for (long long r = warp; r < rows; r += nwarp) {
-    const long long h0 = host_row_offset(d, P, r);
-    const long long d0 = r * nx;
-    for (int x = lane; x < nx; x += 32) {
+    long long q = r;
+    const int j = (int)(q % d.n[1]); q /= d.n[1];
+    const int k = (int)(q % d.n[2]); q /= d.n[2];
+    const int l = (int)(q % d.n[3]); q /= d.n[3];
+    const int n = (int)(q % d.n[4]);
+    const int m = (int)(q / d.n[4]);
+    const long long h0 = RT_ONX + P[0] * ((j + RT_ONX) + P[1] * ((k + RT_ONX) + P[2] *
+                         ((l + RT_ONX) + P[3] * ((n + RT_ONX) + P[4] * (long long)(m + RT_ONX)))));
+    const long long d0 = r * d.n[0];
+    for (int x = lane; x < d.n[0]; x += 32) {
       if (TO_DEVICE) ddst[d0 + x] = (T)hsrc[h0 + x];
       else hdst[h0 + x] = (double)dsrc[d0 + x];
     }
   }
 }
 
-// pairs: nx even and at most 64 (a row within one warp pass), the host
-// array on a 16-byte boundary (the padded row starts then are too: RT_ONX
-// and the padded extents are even)
-static int host_paired(const Dims& d, const void* host) {
-  return d.n[0] % 2 == 0 && d.n[0] <= 64 && (reinterpret_cast<uintptr_t>(host) & 15u) == 0;
-}
-
 template <class T>
 cudaError_t launch_host_gather(const double* host, T* dst, const Dims& d, cudaStream_t st) {
-  host_rows_kernel<true, T><<<RT_HOST_BLOCKS, 256, 0, st>>>(host, nullptr, nullptr, dst, d, host_paired(d, host));
+  host_rows_kernel<true, T><<<8 * 152, 256, 0, st>>>(host, nullptr, nullptr, dst, d);
   return cudaGetLastError();
 }
 template <class T>
 cudaError_t launch_host_scatter(const T* src, double* host, const Dims& d, cudaStream_t st) {
-  host_rows_kernel<false, T><<<RT_HOST_BLOCKS, 256, 0, st>>>(nullptr, host, src, nullptr, d, host_paired(d, host));
+  host_rows_kernel<false, T><<<8 * 152, 256, 0, st>>>(nullptr, host, src, nullptr, d);
   return cudaGetLastError();
 }
 template cudaError_t launch_host_gather<double>(const double*, double*, const Dims&, cudaStream_t);

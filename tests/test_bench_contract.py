@@ -44,12 +44,14 @@ def test_fp64_roofline_is_bound_by_the_fp64_pipe():
     import bench
     n = (32,) * 6
     ops = bench.fp64_ops_per_cell("fast", n)
-    # 6 per axis, face 0 once per 32 cells: v*E(0) on the five clamped axes,
-    # a full flux on z with the lower reflection
-    assert abs(ops - (1 + 6 * 6 + (5 * 1 + 4) / 32)) < 1e-12
-    assert abs(bench.fp64_ops_per_cell("fast", n, lower_reflection=False) - (1 + 36 + 6 / 32)) < 1e-12
+    # 6 per axis (5 along x: the lanes of a 32-cell row share their
+    # differences), face 0 once per 32 cells: v*E(0) on the five clamped
+    # axes, a full flux on z with the lower reflection
+    assert abs(ops - (1 + 6 * 6 - 1 + (5 * 1 + 4) / 32)) < 1e-12
+    assert abs(bench.fp64_ops_per_cell("fast", n, lower_reflection=False) - (1 + 35 + 6 / 32)) < 1e-12
     assert bench.fp64_ops_per_cell("split", n) is None
-    assert bench.fp64_ops_per_cell("fast", (8, 1, 1, 1, 1, 8)) == 1 + 2 * (6 + 1 / 8)
+    assert bench.fp64_ops_per_cell("fast", (8, 1, 1, 1, 1, 8)) == 1 + 2 * (6 + 1 / 8) - 1
+    assert abs(bench.fp64_ops_per_cell("fast", (6, 1, 1, 1, 1, 8)) - (1 + 2 * 6 + 1 / 6 + 1 / 8)) < 1e-12
     rf = bench.roofline("fp64", 32 ** 6, 0.1, "step_fp64_split", fp64=(ops, 5e11))
     assert rf["bound"] == "fp64" and rf["unit"] == "G binary64 ops/s"
     assert abs(rf["achieved"] - ops * 32 ** 6 / 0.1 / 1e9) < 0.01
