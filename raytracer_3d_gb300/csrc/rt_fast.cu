@@ -32,27 +32,6 @@ namespace rt {
 
 namespace {
 
-// Division of a 32-bit index n < 2^31 by a divisor fixed for the launch:
-// q = (n * m) >> S with S = 31 + ceil(log2 d) and m = ceil(2^S / d) < 2^32
-// (Granlund and Montgomery, "Division by invariant integers using
-// multiplication", PLDI 1994: the rounding error n*(m - 2^S/d)/2^S stays
-// below 1/d for n < 2^31, so the quotient is exact).  One wide multiply
-// and one shift instead of a generic division sequence per coordinate.
-struct DivU32 {
-  unsigned d, m, S;
-  __device__ __forceinline__ unsigned div(unsigned n) const {
-    return (unsigned)(((unsigned long long)n * m) >> S);
-  }
-};
-
-DivU32 make_div(unsigned d) {
-  unsigned k = 0;
-  while ((1ull << k) < d) k++;
-  const unsigned S = 31 + k;
-  const unsigned long long m = ((1ull << S) + d - 1) / d;
-  return DivU32{d, (unsigned)m, S};
-}
-
 // 32-bit index geometry of the two passes (the host rejects fields of 2^31
 // cells or more; their flux fields alone would exceed the device memory):
 // strides, the divisors of the cell and band coordinates, and the band

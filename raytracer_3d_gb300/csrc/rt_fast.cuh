@@ -53,6 +53,29 @@ __host__ __device__ __forceinline__ double f64_from_bits(unsigned long long u) {
 #endif
 }
 
+// Division of a 32-bit index n < 2^31 by a divisor 1 <= d < 2^31 fixed
+// for a launch: q = (n * m) >> S with S = 31 + ceil(log2 d) and
+// m = ceil(2^S / d) < 2^32 (Granlund and Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994: the rounding error
+// n*(m - 2^S/d)/2^S stays below 1/d for n < 2^31, so the quotient is
+// exact).  One wide multiply and one shift instead of a generic division
+// sequence per coordinate; checked on the host against n / d
+// (tests/native/fastdiv_check.cu).
+struct DivU32 {
+  unsigned d, m, S;
+  __host__ __device__ __forceinline__ unsigned div(unsigned n) const {
+    return (unsigned)(((unsigned long long)n * m) >> S);
+  }
+};
+
+inline DivU32 make_div(unsigned d) {
+  unsigned k = 0;
+  while ((1ull << k) < d) k++;
+  const unsigned S = 31 + k;
+  const unsigned long long m = ((1ull << S) + d - 1) / d;
+  return DivU32{d, (unsigned)m, S};
+}
+
 // v > 0 for a binary64 v that is not NaN, on the integer pipe: the bit
 // pattern read as a signed integer is positive exactly for v > +0
 __host__ __device__ __forceinline__ bool f64_pos(double v) { return (long long)f64_bits(v) > 0; }

@@ -52,6 +52,23 @@ def test_fast_superbee_selection_is_exact():
         assert " 0 failures" in r.stdout
 
 
+def test_fast_index_division_is_exact():
+    """the fast binary64 step's coordinates divide by invariant divisors
+    through one wide multiply and a shift; the quotient equals n / d for
+    every divisor up to 70000 and sampled larger ones, at the boundary
+    numerators and random ones below 2^31"""
+    with tempfile.TemporaryDirectory() as tmp:
+        out = os.path.join(tmp, "fastdiv_check")
+        cmd = [_nvcc(), "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC,
+               os.path.join(HERE, "native", "fastdiv_check.cu"), "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout + r.stderr
+        r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+        print(r.stdout)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert " 0 failures" in r.stdout
+
+
 def test_binary32_update_rounds_without_bias():
     """the binary32 update's stochastic rounding returns a neighbour of the
     exact sum and has zero mean error over the random words, also for
