@@ -194,7 +194,9 @@ int rt_get_tendency(rt_handle* h, double* dE, double* meanfl);
  *        slope selected exactly, update regrouped; 8 more bytes per cell);
  *        within a few units in the last place of the reference's result per
  *        step, NOT bit-identical to it.  band = m values per band of its
- *        spectral-plane order (1: natural order)
+ *        spectral-plane order (1: natural order; a width that does not
+ *        divide nm is reduced to the largest one that does); fields of
+ *        2^31 cells or more are rejected (RT_ERR_CUDA on the step)
  * Every other variant gives the same result: bit-identical to the
  * reference's arithmetic in binary64, and among themselves in binary32.
  * band: values per band of the plane schedule (default 8); threads: CTA
