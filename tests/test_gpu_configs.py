@@ -34,7 +34,7 @@ def _built():
     g.build()
 
 
-def test_config2_schedules_agree_at_32():
+def test_jet_large_schedules_agree_at_32e6():
     exp = configs.jet_large()
     m = configs.build_model(exp, "fp64", padded=False)
     try:
@@ -54,7 +54,7 @@ def test_config2_schedules_agree_at_32():
         m.close()
 
 
-def test_config2_cells_against_the_oracle_at_32():
+def test_jet_large_cells_against_the_oracle_at_32e6():
     """1500 cells of one bit-exact step at 32^6 (half of them on a boundary
     plane: open faces, z walls under reflection, the edges of the spectral
     axes) against the oracle's per-cell restatement of the reference's
@@ -89,7 +89,7 @@ def test_config2_cells_against_the_oracle_at_32():
         m.close()
 
 
-def test_config3_fp32_1000_steps_at_32():
+def test_jet_large_fp32_1000_steps_at_32e6():
     exp = configs.jet_large()
     steps = 1000
     m64 = configs.build_model(exp, "fp64", padded=False)
@@ -120,7 +120,7 @@ def test_config3_fp32_1000_steps_at_32():
     assert drift <= FP32_DRIFT_TOL
 
 
-def test_config4_ensemble_500_steps_against_fp64():
+def test_ensemble48_fp32_500_steps_against_fp64():
     from raytracer_3d_gb300.batch import Batch
     rng = np.random.default_rng(2024)
     exps = [configs.ensemble_member(rng, steps=500) for _ in range(48)]

@@ -169,7 +169,7 @@ def _vol(o, n):
     return vol
 
 
-def test_config1_packet_200_steps():
+def test_packet_8x8x16x16e3_200_steps():
     """the 8x8x16 x 16^3 packet workload run to its full 200 steps: the
     two-pass bit-exact schedule equals the oracle bit for bit at every
     snapshot step, the fast schedule stays within 1e-12 relative L-infinity,
@@ -217,7 +217,7 @@ def test_config1_packet_200_steps():
         e_fast = float(np.sum(fast.E[sl] * vol))
         assert e_exact == e_ref
         assert abs(e_fast - e_ref) <= 1e-12 * abs(e_ref)
-        print("config 1, 200 steps: split bit-identical at %s; fast within %.2e (L-inf), energy %.3e (rel); "
+        print("packet 8x8x16x16^3, 200 steps: split bit-identical at %s; fast within %.2e (L-inf), energy %.3e (rel); "
               "residual %.2e of %.2e" % (checks, worst, abs(e_fast - e_ref) / abs(e_ref), b["residual"], scale))
     finally:
         exact.close()
